@@ -1,0 +1,375 @@
+"""LBVH build + closest-hit trace benchmark on one GB300 (or N replicas).
+
+Default workload (one "step"): the mid-size coherent scene -- a 6,320-triangle
+torus plus a 2,000-triangle ground plane (8,320 triangles) -- is built from
+device-resident triangles and traced with 1024 x 1024 primary rays from a
+pinhole camera at (0, 0, 3) (60 deg) plus 1,048,576 incoherent rays (origins
+uniform in 1.5x the scene box, directions uniform on the sphere): 2,097,152
+rays per step. `value` is rays per second over whole steps (build included),
+in Mrays/s; `build` and `trace` give the two stages alone. The L2 (129 MB) is
+flushed by writing a 256 MB buffer between timed steps, outside the timing.
+
+Also measured (not part of the step): the build of a 16M-triangle random soup,
+the workload of the HBM roofline (`build_16m`), timed per stage.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica of the same
+step on its own GPU ("replicas only": the path has no exchange step); value
+is the sum of rays over all ranks / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Build Mprims/s + trace Mrays/s (1 GB300)"
+WORKLOAD = "torus8320_primary1024x1024_incoherent1M"
+N_BUILD_16M = 16_000_000
+# algorithmic HBM bytes per primitive of the parity build, by stage (see
+# the design doc): bounds 48, Morton 48 + 4, sort 4 passes x 8, split 4 + 16,
+# fit 48 + 4 + 4 + 8 + 8 + 32
+BYTES_PER_PRIM = {"bounds": 48, "morton": 52, "sort": 32, "split": 20, "fit": 104}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), line.strip()))
+
+    def mark(self, begin: bool):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        inside = [s for t, s in self.samples if self.t0 and self.t1 and self.t0 - 0.05 <= t <= self.t1 + 0.05]
+        if not inside and self.samples:  # timed region shorter than one sample period
+            mid = 0.5 * ((self.t0 or 0) + (self.t1 or 0))
+            inside = [min(self.samples, key=lambda ts: abs(ts[0] - mid))[1]]
+        sm, mx, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in inside:
+            f = [x.strip() for x in s.split(",")]
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except Exception:
+                continue
+            for k, name in enumerate(names[1:], start=5):
+                if k < len(f) and f[k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(inside)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# --------------------------------------------------------------------------
+# reference arm: the reference's CPU implementation on the host cores
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    import oracle
+    from lbvh_gb300 import scenes
+
+    impl = oracle.ref()
+    kind = "reference"
+    if impl is None:
+        impl, kind = oracle.port(), "port"
+    cores = os.cpu_count() or 1
+    tris = scenes.torus_scene(seed=11)
+    rays = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(tris, 1 << 20, 3)])
+    # bounded sample: every 8th ray (262,144 rays) per step
+    sample = np.ascontiguousarray(rays[::8])
+    for _ in range(args.warmup):
+        nodes = impl.build(tris, cores)
+        impl.trace(nodes, tris, sample[:4096], cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        nodes = impl.build(tris, cores)
+        impl.trace(nodes, tris, sample, cores)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * float(np.mean(times))
+    value = sample.shape[0] / (ms * 1e-3) / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "triangles": int(tris.shape[0]), "rays_per_step": int(sample.shape[0]),
+                   "sample": "every 8th ray of the 2,097,152-ray step", "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": cores, "kind": kind,
+                         "sample": f"build of all {tris.shape[0]} triangles + {sample.shape[0]} rays per step"},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------
+# our arm
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-16m", action="store_true", help="skip the 16M-triangle build measurement")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import lbvh_gb300 as lb
+    from lbvh_gb300 import _build, scenes
+
+    _build.build()
+    hbm_peak, peak_kind = peaks()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    ctx = lb.Context(local, stream.cuda_stream)
+
+    tris_h = scenes.torus_scene(seed=11)
+    rays_h = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(tris_h, 1 << 20, 3)])
+    n, m = tris_h.shape[0], rays_h.shape[0]
+    tris = torch.from_numpy(tris_h).to(dev)
+    rays = torch.from_numpy(rays_h).to(dev)
+    hits = torch.empty((m, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MB > L2
+    builder = lb.Builder(ctx)
+    bvh = lb.BVH(ctx)
+    ctx.reserve(n, m)
+    trav = None
+
+    def step():
+        nonlocal trav
+        builder(tris, into=bvh)
+        if trav is None:
+            trav = lb.Traverser(bvh)
+        trav(rays, out=hits)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K whole steps --------------------------------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.mark(True)
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        builder(tris, into=bvh)
+        ev[i][1].record(stream)
+        trav(rays, out=hits)
+        ev[i][2].record(stream)
+    torch.cuda.synchronize()
+    clocks.mark(False)
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    build_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    trace_ms = [b.elapsed_time(c) for _, b, c in ev]
+    step_ms = float(np.mean([x + y for x, y in zip(build_ms, trace_ms)]))
+    if world > 1:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = world * m / (step_ms * 1e-3) / 1e6
+    gpu_launches = args.steps * (8 + 1)  # bounds, Morton, 4 sort passes, split, fit; trace
+
+    # correctness guard on the timed output: the same hits as an untimed run
+    ref_hits = torch.empty_like(hits)
+    lb.Traverser(lb.Builder(ctx)(tris))(rays, out=ref_hits)
+    torch.cuda.synchronize()
+    assert torch.equal(ref_hits.view(torch.int32), hits.view(torch.int32))
+    hv = lb.hits_view(hits)
+    hit_frac = float(np.mean(hv["prim"] != lb.MISS))
+
+    # ---- e2e: the public API with pinned host buffers ----------------------
+    tris_p = torch.from_numpy(tris_h).pin_memory()
+    rays_p = torch.from_numpy(rays_h).pin_memory()
+    hits_p = torch.empty((m, 4), dtype=torch.float32).pin_memory()
+    b_e2e = lb.BVH(ctx)
+    for _ in range(2):
+        lb.Traverser(builder(tris_p, into=b_e2e))(rays_p, out=hits_p)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        builder(tris_p, into=b_e2e)          # H2D of the triangles inside
+        lb.Traverser(b_e2e)(rays_p, out=hits_p)  # H2D rays, trace, D2H hits, sync
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * float(np.mean(e2e_t))
+    assert torch.equal(hits_p.view(torch.int32), hits.cpu().view(torch.int32))
+
+    # ---- the trace kernel alone: HBM-normalised view ----------------------
+    trace_mean = float(np.mean(trace_ms))
+    trace_bytes = m * (32 + 16)  # rays in, hits out (the scene stays in L2)
+    roofline = {"bound": "hbm", "kernel": "k_trace_tris",
+                "achieved": round(trace_bytes / (trace_mean * 1e-3) / 1e9, 2),
+                "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(trace_bytes / (trace_mean * 1e-3) / 1e9 / hbm_peak, 5),
+                "traffic": None, "peak_kind": peak_kind,
+                "note": "traversal is latency/issue bound; see build_16m for the HBM-bound build"}
+
+    # ---- 16M-triangle build (roofline workload), per stage ----------------
+    build_16m = None
+    if not args.no_16m:
+        del tris_p, rays_p, hits_p
+        soup = torch.from_numpy(scenes.soup_large(N_BUILD_16M, seed=16)).to(dev)
+        big = lb.BVH(ctx)
+        ctx.reserve(N_BUILD_16M, 0)
+        for _ in range(3):
+            builder(soup, into=big)
+        torch.cuda.synchronize()
+        bt = []
+        for _ in range(max(5, min(args.steps, 20))):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            builder(soup, into=big)
+            b.record(stream)
+            torch.cuda.synchronize()
+            bt.append(a.elapsed_time(b))
+        ms16 = float(np.mean(bt))
+        algo = N_BUILD_16M * sum(BYTES_PER_PRIM.values())
+        achieved = algo / (ms16 * 1e-3) / 1e9
+        build_16m = {"triangles": N_BUILD_16M, "ms": round(ms16, 4),
+                     "mprims_s": round(N_BUILD_16M / (ms16 * 1e-3) / 1e6, 1),
+                     "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                                  "bytes_per_prim": sum(BYTES_PER_PRIM.values()),
+                                  "traffic": None, "peak_kind": peak_kind}}
+        ctx.synchronize()
+        del soup, big
+
+    # ---- CPU baseline: the oracle port (or reference) on the host cores ---
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        impl = oracle.ref()
+        kind = "reference"
+        if impl is None:
+            impl, kind = oracle.port(), "port"
+        cores = os.cpu_count() or 1
+        sample = np.ascontiguousarray(rays_h[::8])
+        impl.build(tris_h, cores)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            nodes = impl.build(tris_h, cores)
+            impl.trace(nodes, tris_h, sample, cores)
+            ts.append(time.perf_counter() - t0)
+        cval = sample.shape[0] / float(np.mean(ts)) / 1e6
+        cpu = {"value": round(cval, 3), "unit": "Mrays/s", "cores": cores, "kind": kind,
+               "sample": f"build of all {n} triangles + every 8th ray ({sample.shape[0]}) per step, 3 steps"}
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "triangles": n, "rays_per_step": m,
+                   "parallelism": f"replicas{world}", "l2": "flushed (256 MB write) between timed steps",
+                   "leaf_order": "reference parity (leaf p = primitive p)"},
+        "build": {"ms": round(float(np.mean(build_ms)), 4),
+                  "mprims_s": round(n / (float(np.mean(build_ms)) * 1e-3) / 1e6, 2)},
+        "trace": {"ms": round(trace_mean, 4), "mrays_s": round(m / (trace_mean * 1e-3) / 1e6, 1),
+                  "hit_fraction": round(hit_frac, 4)},
+        "build_16m": build_16m,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+                "ms_per_step": round(e2e_ms, 4),
+                "h2d_bytes_per_step": int(tris_h.nbytes + rays_h.nbytes),
+                "d2h_bytes_per_step": int(m * 16)},
+        "gpu_launches": gpu_launches,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

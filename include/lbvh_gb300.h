@@ -1,0 +1,175 @@
+/*
+ * lbvh_gb300 -- C ABI of the GB300 LBVH build + closest-hit trace library.
+ *
+ * This is the drop-in boundary for tay10r/lbvh's build and traversal path
+ * (header `lbvh.h`). The reference is a header-only C++ template library
+ * whose interface is lbvh::builder<float> (lbvh.h:312-353), lbvh::bvh<float>
+ * (lbvh.h:259-299) and lbvh::traverser (lbvh.h:502-534); every entry point
+ * below names the reference function it replaces. The C++ header
+ * lbvh_gpu.hpp wraps these functions behind the reference's own types.
+ *
+ * Data layouts are the reference's:
+ *   triangle   12 float32 {p0, e0 = a - b, e1 = c - a, normal}  (lbvh.h:1959-1983)
+ *   box        6 float32 {min.xyz, max.xyz}                      (lbvh.h:208-215)
+ *   node       lbvh_node, 32 bytes                               (lbvh.h:220-255)
+ *   ray        8 float32 {pos, dir, tmin, tmax}                  (lbvh.h:388-401)
+ *   hit        lbvh_hit, 16 bytes {prim, t, u, v}                (lbvh.h:359-382, 2015-2035)
+ *
+ * Pointers: every array argument may be device memory (cudaMalloc, managed)
+ * or host memory (pageable or pinned); the library inspects it. Device
+ * arguments are used in place and the call is asynchronous on the context's
+ * stream. Host inputs are copied in before the call returns; a call that
+ * writes host memory synchronizes the stream before it returns.
+ *
+ * Errors: every function returns an lbvh_status. Device-side failures of an
+ * asynchronous call (a bounded wait that gave up, a malformed tree) are
+ * reported by the next synchronizing call on the same context.
+ *
+ * Threading: a context serializes its work on one CUDA stream; use one
+ * context per host thread. Work on one context must not be issued from two
+ * threads at once.
+ */
+#ifndef LBVH_GB300_H
+#define LBVH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LBVH_API __attribute__((visibility("default")))
+#else
+#define LBVH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lbvh_status
+{
+  LBVH_OK = 0,
+  LBVH_ERR_INVALID_ARG = 1, /* null pointer, n < 2, n too large, bad flags */
+  LBVH_ERR_OOM = 2,         /* device allocation failed */
+  LBVH_ERR_TIMEOUT = 3,     /* a bounded device-side wait expired */
+  LBVH_ERR_DEVICE = 4,      /* CUDA runtime error; see lbvh_ctx_last_error */
+  LBVH_ERR_BAD_TOPOLOGY = 5 /* a node array that is not a binary tree */
+} lbvh_status;
+
+typedef struct lbvh_ctx lbvh_ctx; /* device, stream, workspace */
+typedef struct lbvh_bvh lbvh_bvh; /* one device-resident BVH */
+
+/* lbvh::node<float> (lbvh.h:220-255). left/right with LBVH_LEAF_BIT set are
+ * leaf slots; otherwise they index internal nodes. nodes[0] is the root. */
+typedef struct lbvh_node
+{
+  float lo[3];
+  float hi[3];
+  uint32_t left;
+  uint32_t right;
+} lbvh_node;
+
+/* intersection_container<float, triangle_intersection<float>>
+ * (lbvh.h:359-382, 2015-2035). A miss is {LBVH_MISS, +inf, 0, 0}. */
+typedef struct lbvh_hit
+{
+  uint32_t prim;
+  float t;
+  float u;
+  float v;
+} lbvh_hit;
+
+#define LBVH_LEAF_BIT 0x80000000u
+#define LBVH_MISS 0xffffffffu
+#define LBVH_MAX_PRIMS ((1u << 30) - 1)
+
+/* Build flags. The default (0) is reference parity: leaf slot p holds
+ * primitive p in input order, exactly as the reference's builder does
+ * (lbvh.h:1728-1729, 1855-1862), so the node array is bit-identical to the
+ * reference's. */
+
+/* Leaf slot p holds the p-th primitive in (stable) Morton order: the intended
+ * LBVH. Node array = the reference builder's output for the input permuted
+ * by that order; trace reports original primitive ids. */
+#define LBVH_BUILD_SORTED_LEAVES 0x1u
+/* Keep the per-primitive Morton codes, the sorted codes, the stable sort
+ * permutation and the centroid bounds for lbvh_bvh_curve. */
+#define LBVH_BUILD_KEEP_CURVE 0x2u
+
+/* Library version as major * 10000 + minor * 100 + patch. */
+LBVH_API int lbvh_version(void);
+
+/* Human-readable name of a status code. */
+LBVH_API const char* lbvh_status_string(int status);
+
+/* Creates a context on `device` that issues all its work on `stream` (a
+ * cudaStream_t; NULL is the default stream). No reference counterpart: the
+ * reference's builder owns a CPU task scheduler instead (lbvh.h:312-327). */
+LBVH_API int lbvh_ctx_create(int device, void* stream, lbvh_ctx** out);
+LBVH_API int lbvh_ctx_destroy(lbvh_ctx* ctx);
+/* Waits for the context's stream and reports deferred device errors. */
+LBVH_API int lbvh_ctx_synchronize(lbvh_ctx* ctx);
+/* Message describing the last failure on this context ("" if none). */
+LBVH_API const char* lbvh_ctx_last_error(const lbvh_ctx* ctx);
+/* Grows the context workspace for builds of up to n_prims primitives and
+ * traces of up to n_rays host-side rays, so later calls allocate nothing. */
+LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
+
+/* Replaces the reference triangle constructor triangle<float>(a, b, c)
+ * (lbvh.h:1967-1972) for n triangles: verts is n x 9 float32 (a, b, c),
+ * tris_out is n x 12 float32. Bit-identical to the reference compiled
+ * without FP contraction. */
+LBVH_API int lbvh_make_triangles(lbvh_ctx* ctx, const float* verts, size_t n, float* tris_out);
+
+/* An empty BVH handle; builds reuse its storage. */
+LBVH_API int lbvh_bvh_create(lbvh_ctx* ctx, lbvh_bvh** out);
+LBVH_API int lbvh_bvh_destroy(lbvh_ctx* ctx, lbvh_bvh* bvh);
+
+/* Replaces lbvh::builder<float>::operator()(const triangle<float>*, size_t,
+ * const triangle_aabb_converter<float>&) (lbvh.h:329-345, 1793-1822):
+ * builds `bvh` over n >= 2 triangles. Device `tris` are borrowed by the BVH
+ * (as the reference traverser borrows its primitives, lbvh.h:507-524) and
+ * must outlive it; host `tris` are copied into BVH-owned device memory. */
+LBVH_API int lbvh_build_triangles(lbvh_ctx* ctx, const float* tris, size_t n, uint32_t flags, lbvh_bvh* bvh);
+
+/* Replaces lbvh::builder<float>::operator() with a caller aabb_converter
+ * (lbvh.h:342-345): the caller passes the converted boxes, n x 6 float32.
+ * Same borrowing rule as lbvh_build_triangles. */
+LBVH_API int lbvh_build_boxes(lbvh_ctx* ctx, const float* boxes, size_t n, uint32_t flags, lbvh_bvh* bvh);
+
+/* Refit: recomputes every node box of an existing BVH over new primitive
+ * positions, keeping the topology. No reference entry point (the
+ * reference's fit, builder::fit_boxes lbvh.h:1826-1867, is protected); the
+ * result equals that fit run over the existing nodes. `tris` (`boxes`) must
+ * hold the same number of primitives in the same order as the build input;
+ * it replaces the BVH's primitives. */
+LBVH_API int lbvh_refit_triangles(lbvh_ctx* ctx, lbvh_bvh* bvh, const float* tris);
+LBVH_API int lbvh_refit_boxes(lbvh_ctx* ctx, lbvh_bvh* bvh, const float* boxes);
+
+/* Replaces bvh<float>::size() (lbvh.h:274): n_prims, n_nodes = n_prims - 1. */
+LBVH_API int lbvh_bvh_info(const lbvh_bvh* bvh, size_t* n_prims, size_t* n_nodes, uint32_t* flags);
+/* Replaces bvh<float>::begin()/operator[] (lbvh.h:270-292): copies the
+ * (n_prims - 1) x 32-byte node array to dst (host or device). */
+LBVH_API int lbvh_bvh_nodes(lbvh_ctx* ctx, const lbvh_bvh* bvh, void* dst);
+/* Device address of the node array (valid until the next build/destroy). */
+LBVH_API const void* lbvh_bvh_device_nodes(const lbvh_bvh* bvh);
+/* Intermediate build arrays of a LBVH_BUILD_KEEP_CURVE build: Morton codes
+ * in input order (morton_curve_kernel, lbvh.h:1422-1475), sorted codes
+ * (space_filling_curve::sort, lbvh.h:1126-1134), the stable sort permutation,
+ * and the centroid bounds (6 floats). Any output may be NULL. */
+LBVH_API int lbvh_bvh_curve(lbvh_ctx* ctx, const lbvh_bvh* bvh, uint32_t* codes, uint32_t* sorted_codes,
+                   uint32_t* perm, float* bounds6);
+
+/* Replaces traverser<float, triangle<float>, triangle_intersection<float>>::
+ * operator()(ray, triangle_intersector<float>) (lbvh.h:1869-1942,
+ * 2055-2075) for m rays: rays is m x 8 float32, hits receives m lbvh_hit.
+ * Requires a BVH built from triangles. */
+LBVH_API int lbvh_trace_triangles(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m, void* hits);
+/* Same, also writing per-ray counts of box tests and triangle tests. */
+LBVH_API int lbvh_trace_triangles_counts(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m,
+                                void* hits, uint32_t* n_box, uint32_t* n_tri);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* LBVH_GB300_H */

@@ -1,0 +1,93 @@
+"""ctypes binding of the C ABI in include/lbvh_gb300.h.
+
+Loads the in-tree lbvh_gb300/liblbvh_gb300.so. There is no fallback: if the
+library is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbvh_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "lbvh_gb300.h")
+
+LBVH_OK = 0
+LBVH_ERR_INVALID_ARG = 1
+LBVH_ERR_OOM = 2
+LBVH_ERR_TIMEOUT = 3
+LBVH_ERR_DEVICE = 4
+LBVH_ERR_BAD_TOPOLOGY = 5
+
+LBVH_BUILD_SORTED_LEAVES = 0x1
+LBVH_BUILD_KEEP_CURVE = 0x2
+LEAF_BIT = 0x80000000
+MISS = 0xFFFFFFFF
+
+_P = ctypes.c_void_p
+_S = ctypes.c_size_t
+_U32 = ctypes.c_uint32
+_I = ctypes.c_int
+_PP = ctypes.POINTER(ctypes.c_void_p)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "lbvh_version": (_I, []),
+    "lbvh_status_string": (ctypes.c_char_p, [_I]),
+    "lbvh_ctx_create": (_I, [_I, _P, _PP]),
+    "lbvh_ctx_destroy": (_I, [_P]),
+    "lbvh_ctx_synchronize": (_I, [_P]),
+    "lbvh_ctx_last_error": (ctypes.c_char_p, [_P]),
+    "lbvh_ctx_reserve": (_I, [_P, _S, _S]),
+    "lbvh_make_triangles": (_I, [_P, _P, _S, _P]),
+    "lbvh_bvh_create": (_I, [_P, _PP]),
+    "lbvh_bvh_destroy": (_I, [_P, _P]),
+    "lbvh_build_triangles": (_I, [_P, _P, _S, _U32, _P]),
+    "lbvh_build_boxes": (_I, [_P, _P, _S, _U32, _P]),
+    "lbvh_refit_triangles": (_I, [_P, _P, _P]),
+    "lbvh_refit_boxes": (_I, [_P, _P, _P]),
+    "lbvh_bvh_info": (_I, [_P, ctypes.POINTER(_S), ctypes.POINTER(_S), ctypes.POINTER(_U32)]),
+    "lbvh_bvh_nodes": (_I, [_P, _P, _P]),
+    "lbvh_bvh_device_nodes": (_P, [_P]),
+    "lbvh_bvh_curve": (_I, [_P, _P, _P, _P, _P, _P]),
+    "lbvh_trace_triangles": (_I, [_P, _P, _P, _S, _P]),
+    "lbvh_trace_triangles_counts": (_I, [_P, _P, _P, _S, _P, _P, _P]),
+}
+
+
+class LbvhError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"lbvh status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def declared_symbols() -> list[str]:
+    """Names of every function the public header declares."""
+    with open(HEADER) as f:
+        text = f.read()
+    return re.findall(r"LBVH_API\s+[\w\s\*]+?\b(lbvh_\w+)\s*\(", text)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(the CUDA library has no CPU fallback)"
+            )
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(st: int) -> str:
+    return lib().lbvh_status_string(st).decode()

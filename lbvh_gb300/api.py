@@ -1,0 +1,334 @@
+"""Python host interface over the C ABI, mirroring the reference's API.
+
+Reference (tay10r/lbvh, lbvh.h)            here
+-----------------------------------------  -----------------------------------
+triangle<float>(a, b, c)  (1967-1972)      make_triangles(verts)  (GPU kernel)
+builder<float>            (312-353)        Builder
+  operator()(prims, count, converter)      Builder.__call__(prims, count, converter)
+  triangle_aabb_converter<float> (1988)    TRIANGLES (default converter)
+  user aabb_converter functor (342-345)    any callable, or BOXES for ready boxes
+bvh<float>                (259-299)        BVH (size(), at(i), [i], nodes())
+traverser<float, P, I>    (502-534)        Traverser
+  operator()(ray, triangle_intersector)    Traverser.__call__(rays)
+intersection_container    (359-382)        HIT_DTYPE records {prim, t, u, v}
+
+Arrays may be numpy arrays (host) or torch tensors (host or CUDA); the
+library detects where each one lives. Results for host inputs come back as
+numpy arrays; for CUDA inputs they are written to CUDA tensors.
+
+Error behaviour: the reference has none (everything is noexcept and n < 2 is
+undefined behaviour, lbvh.h:1812, 1835-1838). Here invalid input raises
+ValueError before any work, and device failures raise LbvhError.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import LbvhError
+
+NODE_DTYPE = np.dtype(
+    [("lo", "<f4", (3,)), ("hi", "<f4", (3,)), ("left", "<u4"), ("right", "<u4")]
+)
+HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+LEAF_BIT = _lib.LEAF_BIT
+MISS = _lib.MISS
+
+TRIANGLES = "triangles"  # triangle_aabb_converter<float>
+BOXES = "boxes"          # primitives are already boxes (identity converter)
+
+try:  # torch is plumbing (device memory, streams), not required for host use
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_tensor(x) -> bool:
+    return torch is not None and isinstance(x, torch.Tensor)
+
+
+def _addr(x) -> int:
+    if isinstance(x, np.ndarray):
+        if not x.flags.c_contiguous:
+            raise ValueError("arrays must be C-contiguous")
+        return x.ctypes.data
+    if _is_tensor(x):
+        if not x.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return x.data_ptr()
+    raise TypeError(f"expected a numpy array or torch tensor, got {type(x).__name__}")
+
+
+def _rows(x, width: int, name: str) -> int:
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.float32:
+            raise ValueError(f"{name} must be float32")
+        size = x.size
+    elif _is_tensor(x):
+        if x.dtype != torch.float32:
+            raise ValueError(f"{name} must be float32")
+        size = x.numel()
+    else:
+        raise TypeError(f"{name}: expected a numpy array or torch tensor")
+    if size % width:
+        raise ValueError(f"{name}: {size} floats is not a multiple of {width}")
+    return size // width
+
+
+def _is_cuda(x) -> bool:
+    return _is_tensor(x) and x.is_cuda
+
+
+class Context:
+    """A device + stream + workspace (lbvh_ctx). One per host thread."""
+
+    def __init__(self, device: int | None = None, stream: int | None = None):
+        L = _lib.lib()
+        if device is None:
+            device = torch.cuda.current_device() if (torch is not None and torch.cuda.is_available()) else 0
+        if stream is None and torch is not None and torch.cuda.is_available():
+            stream = torch.cuda.current_stream(device).cuda_stream
+        self.device = device
+        self.stream = stream or 0
+        h = ctypes.c_void_p()
+        st = L.lbvh_ctx_create(device, ctypes.c_void_p(self.stream), ctypes.byref(h))
+        if st != 0:
+            raise LbvhError(st, f"context creation failed: {_lib.status_string(st)}")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, st: int):
+        if st != 0:
+            msg = _lib.lib().lbvh_ctx_last_error(self._h).decode()
+            if st == _lib.LBVH_ERR_INVALID_ARG:
+                raise ValueError(msg)
+            raise LbvhError(st, msg)
+
+    def synchronize(self):
+        self.check(_lib.lib().lbvh_ctx_synchronize(self._h))
+
+    def reserve(self, n_prims: int, n_rays: int = 0):
+        self.check(_lib.lib().lbvh_ctx_reserve(self._h, n_prims, n_rays))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().lbvh_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default: dict[int, Context] = {}
+
+
+def default_context() -> Context:
+    dev = torch.cuda.current_device() if (torch is not None and torch.cuda.is_available()) else 0
+    if dev not in _default:
+        _default[dev] = Context(dev)
+    return _default[dev]
+
+
+def make_triangles(verts, out=None, ctx: Context | None = None):
+    """Reference triangle<float>(a, b, c) for n vertex triples, on the GPU.
+    verts: [n, 9] float32 -> [n, 12] float32 (numpy for host input)."""
+    ctx = ctx or default_context()
+    n = _rows(verts, 9, "verts")
+    if out is None:
+        if _is_cuda(verts):
+            out = torch.empty((n, 12), dtype=torch.float32, device=verts.device)
+        else:
+            out = np.empty((n, 12), np.float32)
+    ctx.check(_lib.lib().lbvh_make_triangles(ctx.handle, _addr(verts), n, _addr(out)))
+    return out
+
+
+class BVH:
+    """A device-resident BVH (lbvh::bvh<float>): n - 1 internal nodes of 32
+    bytes, nodes[0] the root, leaf references flagged by LEAF_BIT."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        h = ctypes.c_void_p()
+        self.ctx.check(_lib.lib().lbvh_bvh_create(self.ctx.handle, ctypes.byref(h)))
+        self._h = h
+        self._keep = None  # keeps borrowed device primitives alive
+        self._host_nodes = None
+        self.kind = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self):
+        n = ctypes.c_size_t()
+        nn = ctypes.c_size_t()
+        fl = ctypes.c_uint32()
+        _lib.lib().lbvh_bvh_info(self._h, ctypes.byref(n), ctypes.byref(nn), ctypes.byref(fl))
+        return n.value, nn.value, fl.value
+
+    @property
+    def num_primitives(self) -> int:
+        return self.info()[0]
+
+    def size(self) -> int:
+        """bvh<float>::size(): the number of internal nodes."""
+        return self.info()[1]
+
+    __len__ = size
+
+    def nodes(self, out=None):
+        """All nodes: a NODE_DTYPE numpy array, or written into `out` (a
+        numpy array or CUDA tensor of (n - 1) * 32 bytes)."""
+        if out is None:
+            out = np.empty(self.size(), NODE_DTYPE)
+        self.ctx.check(_lib.lib().lbvh_bvh_nodes(self.ctx.handle, self._h, _addr(out)))
+        return out
+
+    def device_nodes_ptr(self) -> int:
+        return _lib.lib().lbvh_bvh_device_nodes(self._h) or 0
+
+    def at(self, i: int):
+        """bvh<float>::at(): bounds-checked node access (IndexError)."""
+        if not 0 <= i < self.size():
+            raise IndexError(i)
+        return self[i]
+
+    def __getitem__(self, i):
+        if self._host_nodes is None:
+            self._host_nodes = self.nodes()
+        return self._host_nodes[i]
+
+    def curve(self):
+        """(codes, sorted_codes, stable_perm, centroid_bounds[6]) of a build
+        made with keep_curve=True."""
+        n = self.num_primitives
+        codes = np.empty(n, np.uint32)
+        sc = np.empty(n, np.uint32)
+        perm = np.empty(n, np.uint32)
+        bounds = np.empty(6, np.float32)
+        self.ctx.check(_lib.lib().lbvh_bvh_curve(self.ctx.handle, self._h, _addr(codes), _addr(sc),
+                                                 _addr(perm), _addr(bounds)))
+        return codes, sc, perm, bounds
+
+    def refit(self, primitives):
+        """Recompute all node boxes over moved primitives (same count and
+        order as the build input), keeping the topology."""
+        n = self.num_primitives
+        L = _lib.lib()
+        self._host_nodes = None
+        if self.kind == TRIANGLES:
+            if _rows(primitives, 12, "triangles") != n:
+                raise ValueError("refit needs the build's primitive count")
+            self.ctx.check(L.lbvh_refit_triangles(self.ctx.handle, self._h, _addr(primitives)))
+        else:
+            if _rows(primitives, 6, "boxes") != n:
+                raise ValueError("refit needs the build's primitive count")
+            self.ctx.check(L.lbvh_refit_boxes(self.ctx.handle, self._h, _addr(primitives)))
+        if _is_cuda(primitives):
+            self._keep = primitives
+        return self
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().lbvh_bvh_destroy(self.ctx.handle, self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Builder:
+    """lbvh::builder<float> on the GPU.
+
+    Builder()(triangles)                      reference parity (default)
+    Builder(sorted_leaves=True)(triangles)    intended LBVH: leaves in Morton order
+    Builder()(boxes, converter=BOXES)         caller-converted boxes
+    Builder()(objects, converter=fn)          fn(objects) -> [n, 6] boxes on the host
+    """
+
+    def __init__(self, ctx: Context | None = None, sorted_leaves: bool = False, keep_curve: bool = False):
+        self.ctx = ctx or default_context()
+        self.flags = (_lib.LBVH_BUILD_SORTED_LEAVES if sorted_leaves else 0) | (
+            _lib.LBVH_BUILD_KEEP_CURVE if keep_curve else 0)
+
+    def __call__(self, primitives, count: int | None = None, converter=TRIANGLES, into: BVH | None = None) -> BVH:
+        bvh = into or BVH(self.ctx)
+        bvh._host_nodes = None
+        L = _lib.lib()
+        if callable(converter):
+            boxes = np.ascontiguousarray(converter(primitives), dtype=np.float32).reshape(-1, 6)
+            primitives, converter = boxes, BOXES
+        if converter == TRIANGLES:
+            n = _rows(primitives, 12, "triangles")
+            fn = L.lbvh_build_triangles
+        elif converter == BOXES:
+            n = _rows(primitives, 6, "boxes")
+            fn = L.lbvh_build_boxes
+        else:
+            raise ValueError(f"unknown converter {converter!r}")
+        if count is not None:
+            if count > n:
+                raise ValueError("count exceeds the primitive array")
+            n = count
+        if n < 2:
+            raise ValueError(f"a BVH needs at least 2 primitives (got {n})")
+        self.ctx.check(fn(self.ctx.handle, _addr(primitives), n, self.flags, bvh.handle))
+        bvh.kind = converter
+        bvh._keep = primitives if _is_cuda(primitives) else None
+        return bvh
+
+
+class Traverser:
+    """lbvh::traverser<float, triangle<float>, triangle_intersection<float>>
+    with triangle_intersector<float>: closest hit per ray, bit-identical to
+    the reference. The primitives are the ones the BVH was built over."""
+
+    def __init__(self, bvh: BVH):
+        if bvh.kind != TRIANGLES:
+            raise ValueError("the built-in traverser intersects triangles")
+        self.bvh = bvh
+        self.ctx = bvh.ctx
+
+    def __call__(self, rays, out=None, counts: bool = False):
+        """rays: [m, 8] float32 {pos, dir, tmin, tmax} (or one ray of 8).
+        Returns HIT_DTYPE records (numpy for host rays; for CUDA rays a
+        [m, 4] tensor whose rows view as {prim, t, u, v}). With counts=True
+        also returns per-ray box-test and triangle-test counts."""
+        m = _rows(rays, 8, "rays")
+        cuda = _is_cuda(rays)
+        if out is None:
+            if cuda:
+                out = torch.empty((m, 4), dtype=torch.float32, device=rays.device)
+            else:
+                out = np.empty(m, HIT_DTYPE)
+        L = _lib.lib()
+        if counts:
+            if cuda:
+                nb = torch.empty(m, dtype=torch.int32, device=rays.device)
+                nt = torch.empty(m, dtype=torch.int32, device=rays.device)
+            else:
+                nb = np.empty(m, np.uint32)
+                nt = np.empty(m, np.uint32)
+            self.ctx.check(L.lbvh_trace_triangles_counts(self.ctx.handle, self.bvh.handle, _addr(rays), m,
+                                                         _addr(out), _addr(nb), _addr(nt)))
+            return out, nb, nt
+        self.ctx.check(L.lbvh_trace_triangles(self.ctx.handle, self.bvh.handle, _addr(rays), m, _addr(out)))
+        return out
+
+
+def hits_view(t) -> np.ndarray:
+    """HIT_DTYPE view of a [m, 4] float32 hits tensor copied to the host."""
+    a = t.detach().cpu().numpy() if _is_tensor(t) else np.asarray(t)
+    return np.ascontiguousarray(a).view(HIT_DTYPE).reshape(-1)

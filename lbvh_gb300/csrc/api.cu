@@ -1,0 +1,722 @@
+// C ABI (include/lbvh_gb300.h): contexts, workspace, BVH handles, and the
+// build / refit / trace entry points that replace the reference's
+// lbvh::builder<float>, lbvh::bvh<float> and lbvh::traverser.
+#include "../../include/lbvh_gb300.h"
+
+#include "build.cuh"
+#include "trace.cuh"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+using namespace lbvh_gb300;
+
+namespace {
+
+struct DevBuf
+{
+  void* ptr = nullptr;
+  size_t cap = 0;
+};
+
+size_t
+align_up(size_t x, size_t a)
+{
+  return (x + a - 1) / a * a;
+}
+
+} // namespace
+
+struct lbvh_ctx
+{
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 1;
+  BuildState* state = nullptr; // persistent: holds the sticky error word
+  uint32_t* h_err = nullptr;   // pinned readback of state->error
+  DevBuf ws;                   // build workspace arena
+  size_t ws_prims = 0;         // primitives the arena is laid out for
+  BuildBuffers bufs{};
+  DevBuf flags;                // arrival counters, even between builds
+  DevBuf lookback;             // radix sort look-back words (epoch-tagged)
+  DevBuf rays;                 // staging for host rays
+  DevBuf hits;                 // staging for host hits
+  DevBuf counts;               // staging for host per-ray counts
+  DevBuf prims_in;             // staging for host refit input
+  uint32_t epoch = 0;          // look-back epoch of the last sort pass
+  char msg[512] = { 0 };
+};
+
+struct lbvh_bvh
+{
+  int device = 0;
+  uint32_t n = 0;
+  uint32_t flags = 0;
+  int kind = 0; // 1 triangles, 2 boxes
+  DevBuf nodes;
+  const void* prims = nullptr; // primitives in input order (borrowed or owned)
+  DevBuf prims_owned;
+  DevBuf sorted_prims;         // sorted-leaf mode: primitives in leaf order
+  DevBuf leaf_prim;            // sorted-leaf mode: leaf slot -> primitive id
+  DevBuf curve;                // keep-curve: codes, sorted codes, perm, bounds
+};
+
+namespace {
+
+constexpr int kKindTris = 1;
+constexpr int kKindBoxes = 2;
+
+int
+fail(lbvh_ctx* c, int status, const char* fmt, ...)
+{
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->msg, sizeof(c->msg), fmt, ap);
+    va_end(ap);
+  }
+  return status;
+}
+
+int
+cuda_fail(lbvh_ctx* c, cudaError_t e, const char* what)
+{
+  const int st = (e == cudaErrorMemoryAllocation) ? LBVH_ERR_OOM : LBVH_ERR_DEVICE;
+  cudaGetLastError();
+  return fail(c, st, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                                                             \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return cuda_fail(c, e_, what);                                                               \
+  } while (0)
+
+bool
+on_device(const void* p)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Grow-only stream-ordered buffer.
+cudaError_t
+reserve(DevBuf& b, size_t bytes, cudaStream_t s, bool* grew = nullptr)
+{
+  if (grew)
+    *grew = false;
+  if (b.cap >= bytes)
+    return cudaSuccess;
+  if (b.ptr) {
+    cudaError_t e = cudaFreeAsync(b.ptr, s);
+    b.ptr = nullptr;
+    b.cap = 0;
+    if (e != cudaSuccess)
+      return e;
+  }
+  const size_t want = align_up(bytes, 1 << 16);
+  cudaError_t e = cudaMallocAsync(&b.ptr, want, s);
+  if (e != cudaSuccess) {
+    b.ptr = nullptr;
+    return e;
+  }
+  b.cap = want;
+  if (grew)
+    *grew = true;
+  return cudaSuccess;
+}
+
+void
+release(DevBuf& b, cudaStream_t s)
+{
+  if (b.ptr)
+    cudaFreeAsync(b.ptr, s);
+  b.ptr = nullptr;
+  b.cap = 0;
+}
+
+uint32_t
+bounds_blocks_for(const lbvh_ctx* c, uint32_t n)
+{
+  const uint32_t want = ceil_div_u32(n, kBoundsThreads * 8);
+  const uint32_t cap = uint32_t(c->num_sms) * 4;
+  return want < 1 ? 1 : (want > cap ? cap : want);
+}
+
+uint32_t
+morton_blocks_for(const lbvh_ctx* c, uint32_t n)
+{
+  const uint32_t want = ceil_div_u32(n, kMortonThreads);
+  const uint32_t cap = uint32_t(c->num_sms) * 8;
+  return want < 1 ? 1 : (want > cap ? cap : want);
+}
+
+// Lays out the build arena for n primitives and the arrival flags.
+int
+ws_reserve(lbvh_ctx* c, size_t n)
+{
+  const size_t tiles = (n + kSortTile - 1) / kSortTile;
+  const size_t A = 256;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align_up(off + bytes, A);
+    return o;
+  };
+  const size_t o_part = take(size_t(c->num_sms) * 4 * 48);
+  const size_t o_ka = take(4 * n);
+  const size_t o_kb = take(4 * n);
+  const size_t o_va = take(4 * n);
+  const size_t o_vb = take(4 * n);
+  const size_t o_child = take(8 * n);
+  const size_t o_lp = take(4 * n);
+  const size_t o_np = take(4 * n);
+  CK(reserve(c->ws, off, c->stream), "workspace allocation");
+  // The look-back buffer only ever holds look-back words: fresh words read as
+  // "not published" (epoch 0 is never used), so it is cleared only on growth.
+  bool grew = false;
+  CK(reserve(c->lookback, tiles * 256 * 8, c->stream, &grew), "look-back allocation");
+  if (grew)
+    CK(cudaMemsetAsync(c->lookback.ptr, 0, c->lookback.cap, c->stream), "look-back clear");
+  if (c->flags.cap < 4 * n) {
+    CK(reserve(c->flags, 4 * n, c->stream), "flag allocation");
+    CK(cudaMemsetAsync(c->flags.ptr, 0, c->flags.cap, c->stream), "flag clear");
+  }
+  char* base = static_cast<char*>(c->ws.ptr);
+  BuildBuffers& b = c->bufs;
+  b.state = c->state;
+  b.partials = base + o_part;
+  b.keys_a = reinterpret_cast<uint32_t*>(base + o_ka);
+  b.keys_b = reinterpret_cast<uint32_t*>(base + o_kb);
+  b.vals_a = reinterpret_cast<uint32_t*>(base + o_va);
+  b.vals_b = reinterpret_cast<uint32_t*>(base + o_vb);
+  b.lookback = static_cast<unsigned long long*>(c->lookback.ptr);
+  b.child = reinterpret_cast<uint2*>(base + o_child);
+  b.leaf_parent = reinterpret_cast<uint32_t*>(base + o_lp);
+  b.node_parent = reinterpret_cast<uint32_t*>(base + o_np);
+  b.flags = static_cast<uint32_t*>(c->flags.ptr);
+  c->ws_prims = n;
+  return LBVH_OK;
+}
+
+// Next look-back epoch base (4 passes per sort). Epoch 0 means "never
+// written"; on wrap-around the look-back words are cleared.
+int
+next_epoch(lbvh_ctx* c, uint32_t* base)
+{
+  if (c->epoch == 0 || c->epoch > 0xfffffff0u) {
+    if (c->epoch != 0 && c->lookback.ptr)
+      CK(cudaMemsetAsync(c->lookback.ptr, 0, c->lookback.cap, c->stream), "look-back clear");
+    c->epoch = 4;
+  }
+  *base = c->epoch;
+  c->epoch += 4;
+  return LBVH_OK;
+}
+
+// Reads and clears the sticky device error word after a stream sync.
+int
+check_device(lbvh_ctx* c)
+{
+  CK(cudaMemcpyAsync(c->h_err, &c->state->error, 4, cudaMemcpyDeviceToHost, c->stream), "status read");
+  CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+  const uint32_t err = *c->h_err;
+  if (!err)
+    return LBVH_OK;
+  CK(cudaMemsetAsync(&c->state->error, 0, 4, c->stream), "status clear");
+  // an interrupted build can leave arrival flags odd: start them over
+  if (c->flags.ptr)
+    CK(cudaMemsetAsync(c->flags.ptr, 0, c->flags.cap, c->stream), "flag clear");
+  CK(cudaMemsetAsync(c->state, 0, offsetof(BuildState, error), c->stream), "state clear");
+  CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+  if (err & kErrLookbackTimeout)
+    return fail(c, LBVH_ERR_TIMEOUT, "radix sort look-back wait expired");
+  if (err & kErrFitTimeout)
+    return fail(c, LBVH_ERR_TIMEOUT, "box fit wait expired");
+  return fail(c, LBVH_ERR_BAD_TOPOLOGY, "node array is not a binary tree over its leaves");
+}
+
+int
+set_device(lbvh_ctx* c)
+{
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  return LBVH_OK;
+}
+
+// Shared build body for triangles and boxes.
+int
+build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh* bvh, int kind)
+{
+  if (!c || !prims || !bvh)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (n < 2 || n > kMaxPrims)
+    return fail(c, LBVH_ERR_INVALID_ARG, "primitive count %zu outside [2, %u]", n, kMaxPrims);
+  if (flags & ~(LBVH_BUILD_SORTED_LEAVES | LBVH_BUILD_KEEP_CURVE))
+    return fail(c, LBVH_ERR_INVALID_ARG, "unknown build flags 0x%x", flags);
+  int st = set_device(c);
+  if (st)
+    return st;
+  const uint32_t nn = uint32_t(n);
+  const size_t rec = (kind == kKindTris) ? sizeof(Tri) : sizeof(Box);
+
+  const void* dprims = prims;
+  if (!on_device(prims)) {
+    CK(reserve(bvh->prims_owned, rec * n, c->stream), "primitive allocation");
+    CK(cudaMemcpyAsync(bvh->prims_owned.ptr, prims, rec * n, cudaMemcpyHostToDevice, c->stream), "primitive upload");
+    dprims = bvh->prims_owned.ptr;
+  }
+  if (kind == kKindTris && (reinterpret_cast<uintptr_t>(dprims) & 15))
+    return fail(c, LBVH_ERR_INVALID_ARG, "device triangles must be 16-byte aligned");
+  if (kind == kKindBoxes && (reinterpret_cast<uintptr_t>(dprims) & 7))
+    return fail(c, LBVH_ERR_INVALID_ARG, "device boxes must be 8-byte aligned");
+
+  if ((st = ws_reserve(c, n)))
+    return st;
+  CK(reserve(bvh->nodes, sizeof(Node) * (n - 1), c->stream), "node allocation");
+  BuildBuffers& b = c->bufs;
+  b.bounds_blocks = bounds_blocks_for(c, nn);
+  b.morton_blocks = morton_blocks_for(c, nn);
+  const bool keep = flags & LBVH_BUILD_KEEP_CURVE;
+  const bool sorted_leaves = flags & LBVH_BUILD_SORTED_LEAVES;
+
+  if (kind == kKindTris)
+    CK(launch_curve_tris(static_cast<const Tri*>(dprims), nn, b, c->stream), "curve launch");
+  else
+    CK(launch_curve_boxes(static_cast<const Box*>(dprims), nn, b, c->stream), "curve launch");
+
+  uint32_t* curve = nullptr;
+  if (keep) {
+    CK(reserve(bvh->curve, 12 * n + 64, c->stream), "curve allocation");
+    curve = static_cast<uint32_t*>(bvh->curve.ptr);
+    CK(cudaMemcpyAsync(curve, b.keys_a, 4 * n, cudaMemcpyDeviceToDevice, c->stream), "curve copy");
+    CK(cudaMemcpyAsync(curve + 3 * n, c->state, 24, cudaMemcpyDeviceToDevice, c->stream), "bounds copy");
+  }
+  uint32_t epoch;
+  if ((st = next_epoch(c, &epoch)))
+    return st;
+  CK(launch_sort(nn, keep || sorted_leaves, epoch, b, c->stream), "sort launch");
+  if (keep) {
+    CK(cudaMemcpyAsync(curve + n, b.keys_a, 4 * n, cudaMemcpyDeviceToDevice, c->stream), "curve copy");
+    CK(cudaMemcpyAsync(curve + 2 * n, b.vals_a, 4 * n, cudaMemcpyDeviceToDevice, c->stream), "curve copy");
+  }
+  Node* nodes = static_cast<Node*>(bvh->nodes.ptr);
+  if (sorted_leaves) {
+    CK(reserve(bvh->sorted_prims, rec * n, c->stream), "sorted primitive allocation");
+    CK(reserve(bvh->leaf_prim, 4 * n, c->stream), "leaf map allocation");
+    CK(cudaMemcpyAsync(bvh->leaf_prim.ptr, b.vals_a, 4 * n, cudaMemcpyDeviceToDevice, c->stream), "leaf map copy");
+    if (kind == kKindTris) {
+      Tri* sp = static_cast<Tri*>(bvh->sorted_prims.ptr);
+      CK(launch_gather_tris(static_cast<const Tri*>(dprims), b.vals_a, nn, sp, c->stream), "gather launch");
+      CK(launch_fit_tris(sp, nn, b, nodes, c->stream), "fit launch");
+    } else {
+      Box* sp = static_cast<Box*>(bvh->sorted_prims.ptr);
+      CK(launch_gather_boxes(static_cast<const Box*>(dprims), b.vals_a, nn, sp, c->stream), "gather launch");
+      CK(launch_fit_boxes(sp, nn, b, nodes, c->stream), "fit launch");
+    }
+  } else {
+    if (kind == kKindTris)
+      CK(launch_fit_tris(static_cast<const Tri*>(dprims), nn, b, nodes, c->stream), "fit launch");
+    else
+      CK(launch_fit_boxes(static_cast<const Box*>(dprims), nn, b, nodes, c->stream), "fit launch");
+  }
+  bvh->n = nn;
+  bvh->flags = flags;
+  bvh->kind = kind;
+  bvh->prims = dprims;
+  bvh->device = c->device;
+  if (!on_device(prims))
+    return check_device(c); // host caller: finish and report before returning
+  return LBVH_OK;
+}
+
+int
+refit_common(lbvh_ctx* c, lbvh_bvh* bvh, const float* prims, int kind)
+{
+  if (!c || !bvh || !prims)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (bvh->n < 2 || bvh->kind != kind)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH was not built from this primitive kind");
+  int st = set_device(c);
+  if (st)
+    return st;
+  const uint32_t n = bvh->n;
+  const size_t rec = (kind == kKindTris) ? sizeof(Tri) : sizeof(Box);
+  const bool host = !on_device(prims);
+  const void* dprims = prims;
+  if (host) {
+    CK(reserve(bvh->prims_owned, rec * n, c->stream), "primitive allocation");
+    CK(cudaMemcpyAsync(bvh->prims_owned.ptr, prims, rec * n, cudaMemcpyHostToDevice, c->stream), "primitive upload");
+    dprims = bvh->prims_owned.ptr;
+  }
+  if ((st = ws_reserve(c, n)))
+    return st;
+  Node* nodes = static_cast<Node*>(bvh->nodes.ptr);
+  if (bvh->flags & LBVH_BUILD_SORTED_LEAVES) {
+    const uint32_t* perm = static_cast<const uint32_t*>(bvh->leaf_prim.ptr);
+    if (kind == kKindTris) {
+      Tri* sp = static_cast<Tri*>(bvh->sorted_prims.ptr);
+      CK(launch_gather_tris(static_cast<const Tri*>(dprims), perm, n, sp, c->stream), "gather launch");
+      CK(launch_refit_tris(sp, n, c->bufs, nodes, c->stream), "refit launch");
+    } else {
+      Box* sp = static_cast<Box*>(bvh->sorted_prims.ptr);
+      CK(launch_gather_boxes(static_cast<const Box*>(dprims), perm, n, sp, c->stream), "gather launch");
+      CK(launch_refit_boxes(sp, n, c->bufs, nodes, c->stream), "refit launch");
+    }
+  } else if (kind == kKindTris) {
+    CK(launch_refit_tris(static_cast<const Tri*>(dprims), n, c->bufs, nodes, c->stream), "refit launch");
+  } else {
+    CK(launch_refit_boxes(static_cast<const Box*>(dprims), n, c->bufs, nodes, c->stream), "refit launch");
+  }
+  bvh->prims = dprims;
+  if (host)
+    return check_device(c);
+  return LBVH_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int
+lbvh_version(void)
+{
+  return 100;
+}
+
+const char*
+lbvh_status_string(int s)
+{
+  switch (s) {
+    case LBVH_OK:
+      return "ok";
+    case LBVH_ERR_INVALID_ARG:
+      return "invalid argument";
+    case LBVH_ERR_OOM:
+      return "out of device memory";
+    case LBVH_ERR_TIMEOUT:
+      return "device wait timed out";
+    case LBVH_ERR_DEVICE:
+      return "CUDA error";
+    case LBVH_ERR_BAD_TOPOLOGY:
+      return "malformed tree";
+    default:
+      return "unknown status";
+  }
+}
+
+int
+lbvh_ctx_create(int device, void* stream, lbvh_ctx** out)
+{
+  if (!out)
+    return LBVH_ERR_INVALID_ARG;
+  *out = nullptr;
+  lbvh_ctx* c = new (std::nothrow) lbvh_ctx;
+  if (!c)
+    return LBVH_ERR_OOM;
+  c->device = device;
+  auto bail = [&](cudaError_t e) {
+    const int st = (e == cudaErrorMemoryAllocation) ? LBVH_ERR_OOM : LBVH_ERR_DEVICE;
+    cudaGetLastError();
+    if (c->h_err)
+      cudaFreeHost(c->h_err);
+    if (c->state)
+      cudaFree(c->state);
+    delete c;
+    return st;
+  };
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess)
+    return bail(e);
+  c->stream = static_cast<cudaStream_t>(stream); // NULL: the default stream
+  if ((e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+    return bail(e);
+  if ((e = cudaMalloc(&c->state, sizeof(BuildState))) != cudaSuccess)
+    return bail(e);
+  if ((e = cudaMemset(c->state, 0, sizeof(BuildState))) != cudaSuccess)
+    return bail(e);
+  if ((e = cudaMallocHost(&c->h_err, 64)) != cudaSuccess)
+    return bail(e);
+  *out = c;
+  return LBVH_OK;
+}
+
+int
+lbvh_ctx_destroy(lbvh_ctx* c)
+{
+  if (!c)
+    return LBVH_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  release(c->ws, c->stream);
+  release(c->flags, c->stream);
+  release(c->lookback, c->stream);
+  release(c->rays, c->stream);
+  release(c->hits, c->stream);
+  release(c->counts, c->stream);
+  release(c->prims_in, c->stream);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->state);
+  cudaFreeHost(c->h_err);
+  delete c;
+  return LBVH_OK;
+}
+
+int
+lbvh_ctx_synchronize(lbvh_ctx* c)
+{
+  if (!c)
+    return LBVH_ERR_INVALID_ARG;
+  int st = set_device(c);
+  if (st)
+    return st;
+  return check_device(c);
+}
+
+const char*
+lbvh_ctx_last_error(const lbvh_ctx* c)
+{
+  return c ? c->msg : "null context";
+}
+
+int
+lbvh_ctx_reserve(lbvh_ctx* c, size_t n_prims, size_t n_rays)
+{
+  if (!c)
+    return LBVH_ERR_INVALID_ARG;
+  int st = set_device(c);
+  if (st)
+    return st;
+  if (n_prims >= 2 && (st = ws_reserve(c, n_prims)))
+    return st;
+  if (n_rays) {
+    CK(reserve(c->rays, 32 * n_rays, c->stream), "ray staging allocation");
+    CK(reserve(c->hits, 16 * n_rays, c->stream), "hit staging allocation");
+  }
+  return LBVH_OK;
+}
+
+int
+lbvh_make_triangles(lbvh_ctx* c, const float* verts, size_t n, float* tris_out)
+{
+  if (!c || !verts || !tris_out)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (n > kMaxPrims)
+    return fail(c, LBVH_ERR_INVALID_ARG, "triangle count %zu too large", n);
+  int st = set_device(c);
+  if (st)
+    return st;
+  if (n == 0)
+    return LBVH_OK;
+  const bool hin = !on_device(verts), hout = !on_device(tris_out);
+  const float* dv = verts;
+  float* dt = tris_out;
+  if (hin) {
+    CK(reserve(c->prims_in, 36 * n, c->stream), "staging allocation");
+    CK(cudaMemcpyAsync(c->prims_in.ptr, verts, 36 * n, cudaMemcpyHostToDevice, c->stream), "vertex upload");
+    dv = static_cast<const float*>(c->prims_in.ptr);
+  }
+  if (hout) {
+    CK(reserve(c->hits, 48 * n, c->stream), "staging allocation");
+    dt = static_cast<float*>(c->hits.ptr);
+  } else if (reinterpret_cast<uintptr_t>(dt) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device triangle output must be 16-byte aligned");
+  }
+  CK(launch_make_triangles(dv, uint32_t(n), reinterpret_cast<Tri*>(dt), c->stream), "make_triangles launch");
+  if (hout) {
+    CK(cudaMemcpyAsync(tris_out, dt, 48 * n, cudaMemcpyDeviceToHost, c->stream), "triangle download");
+    return check_device(c);
+  }
+  return hin ? check_device(c) : LBVH_OK;
+}
+
+int
+lbvh_bvh_create(lbvh_ctx* c, lbvh_bvh** out)
+{
+  if (!c || !out)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  *out = new (std::nothrow) lbvh_bvh;
+  if (!*out)
+    return fail(c, LBVH_ERR_OOM, "host allocation failed");
+  (*out)->device = c->device;
+  return LBVH_OK;
+}
+
+int
+lbvh_bvh_destroy(lbvh_ctx* c, lbvh_bvh* b)
+{
+  if (!c || !b)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  set_device(c);
+  release(b->nodes, c->stream);
+  release(b->prims_owned, c->stream);
+  release(b->sorted_prims, c->stream);
+  release(b->leaf_prim, c->stream);
+  release(b->curve, c->stream);
+  delete b;
+  return LBVH_OK;
+}
+
+int
+lbvh_build_triangles(lbvh_ctx* c, const float* tris, size_t n, uint32_t flags, lbvh_bvh* bvh)
+{
+  return build_common(c, tris, n, flags, bvh, kKindTris);
+}
+
+int
+lbvh_build_boxes(lbvh_ctx* c, const float* boxes, size_t n, uint32_t flags, lbvh_bvh* bvh)
+{
+  return build_common(c, boxes, n, flags, bvh, kKindBoxes);
+}
+
+int
+lbvh_refit_triangles(lbvh_ctx* c, lbvh_bvh* bvh, const float* tris)
+{
+  return refit_common(c, bvh, tris, kKindTris);
+}
+
+int
+lbvh_refit_boxes(lbvh_ctx* c, lbvh_bvh* bvh, const float* boxes)
+{
+  return refit_common(c, bvh, boxes, kKindBoxes);
+}
+
+int
+lbvh_bvh_info(const lbvh_bvh* b, size_t* n_prims, size_t* n_nodes, uint32_t* flags)
+{
+  if (!b)
+    return LBVH_ERR_INVALID_ARG;
+  if (n_prims)
+    *n_prims = b->n;
+  if (n_nodes)
+    *n_nodes = b->n ? b->n - 1 : 0;
+  if (flags)
+    *flags = b->flags;
+  return LBVH_OK;
+}
+
+int
+lbvh_bvh_nodes(lbvh_ctx* c, const lbvh_bvh* b, void* dst)
+{
+  if (!c || !b || !dst)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (b->n < 2)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH has not been built");
+  int st = set_device(c);
+  if (st)
+    return st;
+  const bool host = !on_device(dst);
+  CK(cudaMemcpyAsync(dst, b->nodes.ptr, sizeof(Node) * (b->n - 1), cudaMemcpyDefault, c->stream), "node copy");
+  return host ? check_device(c) : LBVH_OK;
+}
+
+const void*
+lbvh_bvh_device_nodes(const lbvh_bvh* b)
+{
+  return b ? b->nodes.ptr : nullptr;
+}
+
+int
+lbvh_bvh_curve(lbvh_ctx* c, const lbvh_bvh* b, uint32_t* codes, uint32_t* sorted_codes, uint32_t* perm, float* bounds6)
+{
+  if (!c || !b)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (!(b->flags & LBVH_BUILD_KEEP_CURVE) || !b->curve.ptr)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH was not built with LBVH_BUILD_KEEP_CURVE");
+  int st = set_device(c);
+  if (st)
+    return st;
+  const size_t n = b->n;
+  const uint32_t* cv = static_cast<const uint32_t*>(b->curve.ptr);
+  bool host = false;
+  void* outs[4] = { codes, sorted_codes, perm, bounds6 };
+  const void* srcs[4] = { cv, cv + n, cv + 2 * n, cv + 3 * n };
+  const size_t sizes[4] = { 4 * n, 4 * n, 4 * n, 24 };
+  for (int k = 0; k < 4; k++) {
+    if (!outs[k])
+      continue;
+    host |= !on_device(outs[k]);
+    CK(cudaMemcpyAsync(outs[k], srcs[k], sizes[k], cudaMemcpyDefault, c->stream), "curve copy");
+  }
+  return host ? check_device(c) : LBVH_OK;
+}
+
+static int
+trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* hits, uint32_t* n_box, uint32_t* n_tri)
+{
+  if (!c || !b || (m && (!rays || !hits)))
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (b->n < 2 || b->kind != kKindTris)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH was not built from triangles");
+  if (m > 0xffffffffull)
+    return fail(c, LBVH_ERR_INVALID_ARG, "ray count %zu too large", m);
+  if (m == 0)
+    return LBVH_OK;
+  int st = set_device(c);
+  if (st)
+    return st;
+  const bool counts = n_box && n_tri;
+  const bool hr = !on_device(rays), hh = !on_device(hits);
+  const bool hc = counts && (!on_device(n_box) || !on_device(n_tri));
+  const float* dr = rays;
+  Hit* dh = static_cast<Hit*>(hits);
+  uint32_t* db = n_box;
+  uint32_t* dt = n_tri;
+  if (hr) {
+    CK(reserve(c->rays, 32 * m, c->stream), "ray staging allocation");
+    CK(cudaMemcpyAsync(c->rays.ptr, rays, 32 * m, cudaMemcpyHostToDevice, c->stream), "ray upload");
+    dr = static_cast<const float*>(c->rays.ptr);
+  } else if (reinterpret_cast<uintptr_t>(rays) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device rays must be 16-byte aligned");
+  }
+  if (hh) {
+    CK(reserve(c->hits, 16 * m, c->stream), "hit staging allocation");
+    dh = static_cast<Hit*>(c->hits.ptr);
+  } else if (reinterpret_cast<uintptr_t>(hits) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device hits must be 16-byte aligned");
+  }
+  if (hc) {
+    CK(reserve(c->counts, 8 * m, c->stream), "count staging allocation");
+    db = static_cast<uint32_t*>(c->counts.ptr);
+    dt = db + m;
+  }
+  const Tri* tris = (b->flags & LBVH_BUILD_SORTED_LEAVES) ? static_cast<const Tri*>(b->sorted_prims.ptr)
+                                                          : static_cast<const Tri*>(b->prims);
+  const uint32_t* leaf_prim =
+    (b->flags & LBVH_BUILD_SORTED_LEAVES) ? static_cast<const uint32_t*>(b->leaf_prim.ptr) : nullptr;
+  CK(launch_trace_tris(static_cast<const Node*>(b->nodes.ptr), tris, leaf_prim, dr, uint32_t(m), dh,
+                       counts ? db : nullptr, counts ? dt : nullptr, c->stream),
+     "trace launch");
+  if (hh)
+    CK(cudaMemcpyAsync(hits, dh, 16 * m, cudaMemcpyDeviceToHost, c->stream), "hit download");
+  if (hc) {
+    CK(cudaMemcpyAsync(n_box, db, 4 * m, cudaMemcpyDefault, c->stream), "count download");
+    CK(cudaMemcpyAsync(n_tri, dt, 4 * m, cudaMemcpyDefault, c->stream), "count download");
+  }
+  if (hr || hh || hc)
+    return check_device(c);
+  return LBVH_OK;
+}
+
+int
+lbvh_trace_triangles(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* hits)
+{
+  return trace_common(c, b, rays, m, hits, nullptr, nullptr);
+}
+
+int
+lbvh_trace_triangles_counts(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* hits,
+                            uint32_t* n_box, uint32_t* n_tri)
+{
+  if (!n_box || !n_tri)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null count output");
+  return trace_common(c, b, rays, m, hits, n_box, n_tri);
+}
+
+} // extern "C"

@@ -1,0 +1,69 @@
+// Build-side launch parameters, workspace views and launchers.
+#pragma once
+
+#include "common.cuh"
+
+#include <utility>
+
+namespace lbvh_gb300 {
+
+constexpr int kBoundsThreads = 256;
+constexpr int kMortonThreads = 256;
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems; // 4096 keys per tile
+constexpr int kSplitThreads = 256;
+constexpr int kFitThreads = 256;
+constexpr uint32_t kSpinLimit = 1u << 22;   // look-back polls before giving up
+constexpr uint32_t kMaxTreeDepth = 64;      // 30-bit codes + 32-bit index tie-break
+constexpr uint32_t kMaxPrims = (1u << 30) - 1; // look-back counts are 30-bit
+
+// Per-leaf box sources for the templated build kernels.
+struct TriLeaf
+{
+  const Tri* tris;
+  __device__ __forceinline__ Box operator()(uint32_t i) const { return load_tri_box(tris, i); }
+};
+
+struct BoxLeaf
+{
+  const Box* boxes;
+  __device__ __forceinline__ Box operator()(uint32_t i) const
+  {
+    const float2* p = reinterpret_cast<const float2*>(boxes + i);
+    const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    return Box{ { a.x, a.y, b.x }, { b.y, c.x, c.y } };
+  }
+};
+
+// Views into the context workspace for one build of n primitives.
+struct BuildBuffers
+{
+  BuildState* state;
+  void* partials;                 // bounds_blocks ArgBox records
+  uint32_t* keys_a;               // codes (input order), then sorted codes
+  uint32_t* keys_b;
+  uint32_t* vals_a;               // sort permutation (pairs mode)
+  uint32_t* vals_b;
+  unsigned long long* lookback;   // tiles x 256 look-back words
+  uint2* child;                   // n-1 {left, right}
+  uint32_t* leaf_parent;          // n
+  uint32_t* node_parent;          // n-1
+  uint32_t* flags;                // n-1 arrival counters (persistent, even)
+  uint32_t bounds_blocks;
+  uint32_t morton_blocks;
+};
+
+cudaError_t launch_make_triangles(const float* verts, uint32_t n, Tri* out, cudaStream_t s);
+cudaError_t launch_curve_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, cudaStream_t s);
+cudaError_t launch_curve_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, cudaStream_t s);
+cudaError_t launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s);
+cudaError_t launch_fit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
+cudaError_t launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
+cudaError_t launch_gather_tris(const Tri* tris, const uint32_t* perm, uint32_t n, Tri* out, cudaStream_t s);
+cudaError_t launch_gather_boxes(const Box* boxes, const uint32_t* perm, uint32_t n, Box* out, cudaStream_t s);
+cudaError_t launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
+cudaError_t launch_refit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
+
+} // namespace lbvh_gb300

@@ -1,0 +1,132 @@
+"""GPU build parity: the CUDA library against the reference's golden outputs
+and against the pinned CPU oracle, bit for bit (Morton codes, sorted codes,
+stable permutation, centroid bounds, node topology and node boxes)."""
+import numpy as np
+import pytest
+
+import lbvh_gb300 as lb
+from lbvh_gb300 import scenes
+from conftest import GOLDEN, load_golden, nodes_equal
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def ctx(lib_built):
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    return lb.Context()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_build_matches_golden(ctx, name):
+    g = load_golden(name)
+    for src in (g["tris"], dev(g["tris"])):  # host and device input
+        bvh = lb.Builder(ctx, keep_curve=True)(src)
+        codes, sc, perm, bounds = bvh.curve()
+        assert np.array_equal(bounds.view(np.uint32), g["bounds"].view(np.uint32))
+        assert np.array_equal(codes, g["codes"])
+        assert np.array_equal(sc, g["sorted_codes"])
+        assert np.array_equal(perm, g["stable_perm"])
+        assert nodes_equal(bvh.nodes(), g["nodes"])
+    # parity build without the curve (key-only sort path)
+    assert nodes_equal(lb.Builder(ctx)(dev(g["tris"])).nodes(), g["nodes"])
+    # sorted-leaf mode = the reference builder over Morton-ordered input
+    assert nodes_equal(lb.Builder(ctx, sorted_leaves=True)(dev(g["tris"])).nodes(), g["sorted_leaf_nodes"])
+    if "user_boxes" in g:
+        b = lb.Builder(ctx)(dev(g["user_boxes"]), converter=lb.BOXES)
+        assert nodes_equal(b.nodes(), g["user_box_nodes"])
+        b = lb.Builder(ctx)(g["user_boxes"], converter=lambda x: x)  # host converter
+        assert nodes_equal(b.nodes(), g["user_box_nodes"])
+
+
+@pytest.mark.parametrize("n", [2, 3, 31, 1000, 4095, 4096, 4097, 8193, 65537, 300_007])
+def test_build_matches_oracle_random(ctx, port, n):
+    t = scenes.soup(n, seed=n)
+    bvh = lb.Builder(ctx, keep_curve=True)(dev(t))
+    codes, sc, perm = port.curve(t, 8)
+    gc, gsc, gperm, gb = bvh.curve()
+    assert np.array_equal(gc, codes)
+    assert np.array_equal(gsc, sc)
+    assert np.array_equal(gperm, perm)
+    assert np.array_equal(gb.view(np.uint32), port.centroid_bounds(t, 8).view(np.uint32))
+    ref_nodes = port.build(t, 8)
+    assert nodes_equal(bvh.nodes(), ref_nodes)
+    assert port.check_bvh(bvh.nodes()) == 0
+    sl = lb.Builder(ctx, sorted_leaves=True)(dev(t))
+    assert nodes_equal(sl.nodes(), port.build(t[perm], 8))
+
+
+def test_rebuild_reuses_storage(ctx, port):
+    # larger then smaller then larger builds into one handle and one context
+    bvh = lb.BVH(ctx)
+    b = lb.Builder(ctx)
+    for n, seed in [(50_000, 1), (777, 2), (120_001, 3), (2, 4), (50_000, 5)]:
+        t = scenes.soup(n, seed)
+        b(dev(t), into=bvh)
+        assert nodes_equal(bvh.nodes(), port.build(t, 8)), n
+
+
+def test_duplicate_heavy_and_degenerate(ctx, port):
+    # all centroids on a coarse lattice: long runs of equal codes
+    v = scenes.soup_vertices(200_000, 9)
+    c = v.reshape(-1, 3, 3).mean(1)
+    v = (v.reshape(-1, 3, 3) - c[:, None] + (np.round(c * 3) / 3)[:, None]).reshape(-1, 9)
+    t = scenes.make_triangles(v)
+    assert nodes_equal(lb.Builder(ctx)(dev(t)).nodes(), port.build(t, 8))
+    # every triangle identical: every code equal
+    t = scenes.make_triangles(np.tile(scenes.soup_vertices(1, 3), (70_000, 1)))
+    assert nodes_equal(lb.Builder(ctx)(dev(t)).nodes(), port.build(t, 8))
+
+
+def test_make_triangles_kernel(ctx, port):
+    v = scenes.soup_vertices(100_003, 21)
+    want = port.make_triangles(v).view(np.uint32)
+    assert np.array_equal(lb.make_triangles(v, ctx=ctx).view(np.uint32), want)
+    got = lb.make_triangles(dev(v), ctx=ctx).cpu().numpy()
+    assert np.array_equal(got.view(np.uint32), want)
+
+
+@pytest.mark.parametrize("sorted_leaves", [False, True])
+def test_refit_matches_oracle(ctx, port, sorted_leaves):
+    t = scenes.soup(40_000, 31)
+    bvh = lb.Builder(ctx, sorted_leaves=sorted_leaves)(dev(t))
+    v = scenes.triangle_vertices(t).reshape(-1, 9).astype(np.float64)
+    v += scenes.normal(31, 7, v.size).reshape(v.shape) * 0.01  # seeded jitter
+    t2 = scenes.make_triangles(v.astype(np.float32))
+    bvh.refit(dev(t2))
+    nodes = bvh.nodes()
+    if sorted_leaves:
+        perm = port.curve(t, 8)[2]
+        want = port.refit(port.build(t[perm], 8), t2[perm])
+    else:
+        want = port.refit(port.build(t, 8), t2)
+    assert nodes_equal(nodes, want)
+    # host-side refit input as well
+    bvh.refit(t2)
+    assert nodes_equal(bvh.nodes(), want)
+
+
+def test_invalid_arguments_raise(ctx):
+    with pytest.raises(ValueError):
+        lb.Builder(ctx)(np.zeros((1, 12), np.float32))
+    with pytest.raises(ValueError):
+        lb.Builder(ctx)(np.zeros((5, 11), np.float32))
+    with pytest.raises(ValueError):
+        lb.Builder(ctx)(np.zeros((4, 12), np.float64))
+
+
+def test_full_size_16m_build_parity(ctx, port):
+    """The 16M-triangle random soup (the roofline workload) against the
+    oracle, bit for bit, plus the reference's structural invariants."""
+    n = 16_000_000
+    t = scenes.soup_large(n, seed=16)
+    d = dev(t)
+    nodes = lb.Builder(ctx)(d).nodes()
+    assert nodes_equal(nodes, port.build(t, 16))
+    assert port.check_bvh(nodes) == 0

@@ -1,0 +1,97 @@
+"""The CPU oracle (oracle/lbvh_oracle.cpp) pinned against outputs of the
+unmodified reference: the committed golden fixtures everywhere, and the
+reference itself (oracle/_ref) where it was built."""
+import numpy as np
+import pytest
+
+import oracle
+from lbvh_gb300 import scenes
+from conftest import GOLDEN, hit_mismatches, load_golden, nodes_equal
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_port_matches_golden_build(port, name):
+    g = load_golden(name)
+    t = g["tris"]
+    assert np.array_equal(port.tri_boxes(t).view(np.uint32), g["boxes"].view(np.uint32))
+    for threads in (1, 3, 8):
+        assert np.array_equal(port.centroid_bounds(t, threads).view(np.uint32), g["bounds"].view(np.uint32))
+        codes, sc, perm = port.curve(t, threads)
+        assert np.array_equal(codes, g["codes"])
+        assert np.array_equal(sc, g["sorted_codes"])
+        assert np.array_equal(perm, g["stable_perm"])
+        assert nodes_equal(port.build(t, threads), g["nodes"])
+    assert nodes_equal(port.build(t[g["stable_perm"]], 4), g["sorted_leaf_nodes"])
+    if "user_boxes" in g:
+        assert nodes_equal(port.build_boxes(g["user_boxes"], 4), g["user_box_nodes"])
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN if n != "soup2000_boxes"])
+def test_port_matches_golden_trace(port, name):
+    g = load_golden(name)
+    hits = port.trace(g["nodes"], g["tris"], g["rays"], threads=4)
+    assert hit_mismatches(hits, g["hits"]).size == 0
+    pt = g["tris"][g["stable_perm"]]
+    hits = port.trace(g["sorted_leaf_nodes"], pt, g["rays"], threads=2)
+    assert hit_mismatches(hits, g["sorted_leaf_hits"]).size == 0
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_trees_satisfy_reference_invariants(port, name):
+    # check_bvh + check_volumes, lbvh_test.cpp:369-518
+    g = load_golden(name)
+    assert port.check_bvh(g["nodes"]) == 0
+    assert port.check_bvh(g["sorted_leaf_nodes"]) == 0
+
+
+def test_check_bvh_catches_planted_errors(port):
+    g = load_golden("soup968")
+    nodes = g["nodes"].copy()
+    assert port.check_bvh(nodes) == 0
+    bad = nodes.copy()
+    bad["left"][5] = bad["left"][6]  # a node referenced twice / a leaf lost
+    assert port.check_bvh(bad) > 0
+    bad = nodes.copy()
+    i = int(np.nonzero((nodes["left"] & oracle.LEAF_BIT) == 0)[0][0])
+    child = nodes["left"][i]
+    bad["lo"][child] -= 10.0  # child box grows beyond its parent
+    assert port.check_bvh(bad) > 0
+
+
+def test_numpy_triangles_match_golden(port):
+    g = load_golden("soup968")
+    v = scenes.soup_vertices(968, seed=1)  # the vertices soup968 was made from
+    assert np.array_equal(scenes.make_triangles(v).view(np.uint32), g["tris"].view(np.uint32))
+    assert np.array_equal(port.make_triangles(v).view(np.uint32), g["tris"].view(np.uint32))
+
+
+def test_port_refit_equals_fresh_fit(port):
+    # refit over the same topology with unmoved primitives reproduces the build
+    g = load_golden("teapot")
+    nodes = g["nodes"].copy()
+    nodes["lo"] = 0
+    nodes["hi"] = 0
+    assert nodes_equal(port.refit(nodes, g["tris"]), g["nodes"])
+
+
+REF = oracle.ref()
+
+
+@pytest.mark.skipif(REF is None, reason="reference not built on this machine")
+@pytest.mark.parametrize("n,seed", [(2, 1), (5, 2), (100, 3), (4097, 4), (20000, 5)])
+def test_port_matches_reference_random(port, n, seed):
+    t = scenes.soup(n, seed)
+    for threads in (1, 8):
+        assert nodes_equal(port.build(t, threads), REF.build(t, threads))
+        for a, b in zip(port.curve(t, threads), REF.curve(t, threads)):
+            assert np.array_equal(a, b)
+    nodes = REF.build(t, 4)
+    rays = np.concatenate([scenes.pinhole_rays(32, 32), scenes.incoherent_rays(t, 1024, seed)])
+    assert hit_mismatches(port.trace(nodes, t, rays, 4), REF.trace(nodes, t, rays, 4)).size == 0
+
+
+@pytest.mark.skipif(REF is None, reason="reference not built on this machine")
+def test_port_matches_reference_boxes():
+    b = scenes.uniform(3, 0, 6 * 3000).reshape(3000, 6).astype(np.float32)
+    boxes = np.concatenate([np.minimum(b[:, :3], b[:, 3:]), np.maximum(b[:, :3], b[:, 3:])], 1)
+    assert nodes_equal(oracle.port().build_boxes(boxes, 4), REF.build_boxes(boxes, 4))

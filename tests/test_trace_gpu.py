@@ -1,0 +1,102 @@
+"""GPU closest-hit parity: hits (primitive id and the bits of t, u, v) and the
+per-ray box/triangle test counts against the reference's golden outputs and
+the pinned CPU oracle. The arithmetic and visiting order are the reference's,
+so the expected mismatch count is zero (the acceptance bar is >= 99.999% of
+ids equal with t within 1e-6 relative)."""
+import numpy as np
+import pytest
+
+import lbvh_gb300 as lb
+from lbvh_gb300 import scenes
+from conftest import GOLDEN, hit_mismatches, load_golden
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def ctx(lib_built):
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    return lb.Context()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def assert_hits_equal(got, want):
+    bad = hit_mismatches(got, want)
+    assert bad.size == 0, f"{bad.size} of {len(want)} rays differ, first {bad[:8]}"
+    hit = want["prim"] != lb.MISS
+    assert np.all(np.isinf(got["t"][~hit]))
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN if n != "soup2000_boxes"])
+def test_trace_matches_golden(ctx, name):
+    g = load_golden(name)
+    bvh = lb.Builder(ctx)(dev(g["tris"]))
+    assert_hits_equal(lb.Traverser(bvh)(g["rays"]), g["hits"])
+    got = lb.hits_view(lb.Traverser(bvh)(dev(g["rays"])))
+    assert_hits_equal(got, g["hits"])
+    # sorted-leaf mode reports original primitive ids
+    sl = lb.Builder(ctx, sorted_leaves=True)(dev(g["tris"]))
+    want = g["sorted_leaf_hits"].copy()
+    hit = want["prim"] != lb.MISS
+    want["prim"][hit] = g["stable_perm"][want["prim"][hit]]
+    assert_hits_equal(lb.Traverser(sl)(g["rays"]), want)
+
+
+def test_config0_full_pinhole(ctx, port):
+    # 968-triangle random soup, 256 x 256 pinhole rays from (0, 0, 3), 60 deg
+    t = scenes.soup(968, seed=1)
+    rays = scenes.pinhole_rays(256, 256)
+    bvh = lb.Builder(ctx)(dev(t))
+    nodes = port.build(t, 8)
+    want, nb, nt = port.trace(nodes, t, rays, 16, counts=True)
+    got, gb, gt = lb.Traverser(bvh)(rays, counts=True)
+    assert_hits_equal(got, want)
+    assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
+
+
+def test_config1_torus_primary_and_incoherent(ctx, port):
+    # 6,320-triangle torus + 2,000-triangle plane; 1024^2 primary and 1M
+    # incoherent rays
+    t = scenes.torus_scene(seed=11)
+    rays = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(t, 1 << 20, 3)])
+    bvh = lb.Builder(ctx)(dev(t))
+    want = port.trace(port.build(t, 8), t, rays, 16)
+    got = lb.hits_view(lb.Traverser(bvh)(dev(rays)))
+    assert_hits_equal(got, want)
+
+
+def test_edge_rays_random_soup(ctx, port):
+    # axis-parallel rays (0 * inf slabs), rays from box planes, finite tmax
+    t = scenes.soup(5000, seed=5)
+    nodes = port.build(t, 8)
+    lo, hi = scenes.scene_box(t)
+    rays = []
+    for axis in range(3):
+        for s in (1.0, -1.0):
+            g = np.linspace(-1.0, 1.0, 33)
+            a, b = np.meshgrid(g, g)
+            o = np.zeros((a.size, 3))
+            o[:, axis] = -2.0 * s
+            o[:, (axis + 1) % 3] = a.reshape(-1)
+            o[:, (axis + 2) % 3] = b.reshape(-1)
+            d = np.zeros_like(o)
+            d[:, axis] = s
+            r = np.zeros((a.size, 8))
+            r[:, 0:3], r[:, 3:6], r[:, 7] = o, d, np.inf
+            rays.append(r)
+    r = np.concatenate(rays).astype(np.float32)
+    r[::3, 7] = 2.0
+    r[1::5, 6] = 1.5
+    bvh = lb.Builder(ctx)(dev(t))
+    assert_hits_equal(lb.Traverser(bvh)(r), port.trace(nodes, t, r, 8))
+
+
+def test_user_box_bvh_has_no_triangle_traverser(ctx):
+    b = lb.Builder(ctx)(np.zeros((4, 6), np.float32), converter=lb.BOXES)
+    with pytest.raises(ValueError):
+        lb.Traverser(b)
