@@ -264,7 +264,7 @@ class Builder:
             _lib.LBVH_BUILD_KEEP_CURVE if keep_curve else 0)
 
     def __call__(self, primitives, count: int | None = None, converter=TRIANGLES, into: BVH | None = None) -> BVH:
-        bvh = into or BVH(self.ctx)
+        bvh = into if into is not None else BVH(self.ctx)
         bvh._host_nodes = None
         L = _lib.lib()
         if callable(converter):
