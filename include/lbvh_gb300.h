@@ -168,6 +168,34 @@ LBVH_API int lbvh_trace_triangles(lbvh_ctx* ctx, const lbvh_bvh* bvh, const floa
 LBVH_API int lbvh_trace_triangles_counts(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m,
                                 void* hits, uint32_t* n_box, uint32_t* n_tri);
 
+/* Largest primitive count lbvh_build_triangles_noalloc accepts. */
+#define LBVH_NOALLOC_MAX_PRIMS 65536u
+
+/* Allocation-free triangle build. No counterpart in the reference (whose
+ * builder always allocates its own node vector, lbvh.h:1812).
+ *
+ * For callers that must not allocate device memory where they build: a
+ * real-time loop that sizes all its buffers up front and forbids cudaMalloc
+ * on its frame path, a plugin whose host application owns the GPU memory
+ * budget, or a process whose device memory is held by another allocator.
+ * The caller passes device triangles (n x 12 float32, 16-byte aligned) and a
+ * device node array of (n - 1) x 32 bytes (32-byte aligned); the result is
+ * bit-identical to lbvh_build_triangles with flags 0. All other memory is a
+ * fixed scratch array inside the library, sized for LBVH_NOALLOC_MAX_PRIMS
+ * primitives (about 1.8 MB, held by every GPU that loads the library until
+ * the process exits); larger n is rejected with LBVH_ERR_INVALID_ARG, as are
+ * host pointers. The call allocates nothing and does not synchronize: work
+ * is queued on `stream` (a cudaStream_t, NULL = default stream) on the
+ * current device. If d_status is not NULL it receives, in stream order, the
+ * build's device error bits (0 = success).
+ *
+ * The first call on each device looks up the scratch array's device address;
+ * make it before capturing any stream. Every call on a device shares the one
+ * scratch array: calls whose GPU work overlaps (other streams, other threads)
+ * race and corrupt each other, so serialize them per device. */
+LBVH_API int lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint32_t* d_status,
+                                          void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

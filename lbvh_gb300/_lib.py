@@ -20,6 +20,7 @@ LBVH_ERR_TIMEOUT = 3
 LBVH_ERR_DEVICE = 4
 LBVH_ERR_BAD_TOPOLOGY = 5
 
+NOALLOC_MAX_PRIMS = 65536
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000
@@ -53,6 +54,7 @@ SIGNATURES = {
     "lbvh_bvh_curve": (_I, [_P, _P, _P, _P, _P, _P]),
     "lbvh_trace_triangles": (_I, [_P, _P, _P, _S, _P]),
     "lbvh_trace_triangles_counts": (_I, [_P, _P, _P, _S, _P, _P, _P]),
+    "lbvh_build_triangles_noalloc": (_I, [_P, _S, _P, _P, _P]),
 }
 
 

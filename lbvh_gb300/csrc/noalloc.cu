@@ -1,0 +1,173 @@
+// Allocation-free triangle build: lbvh_build_triangles_noalloc.
+//
+// Who needs this: some callers cannot allocate device memory at the point
+// where they want a BVH -- a real-time render or simulation loop that sizes
+// every buffer at start-up and forbids cudaMalloc on its frame path (cudaMalloc
+// can synchronize the device and take milliseconds), a plugin running inside
+// a host application that owns the GPU memory budget and hands the plugin
+// only fixed buffers, or a process whose device memory is already held by
+// another framework's caching allocator. They pass the triangles and the node
+// array; everything else the build needs lives in one file-scope device array
+// below.
+//
+// The scratch array is fixed at kNoAllocMaxPrims primitives (about 1.8 MB).
+// Every GPU that loads this library reserves it until the process exits.
+// All calls on a device share it and it keeps the last call's contents, so
+// each call clears the parts that must start at zero (the build counters, the
+// error word and the arrival flags). Calls whose work overlaps on the GPU --
+// two streams, or two host threads -- race on the array and corrupt each
+// other's results: serialize them per device.
+//
+// Set-up: the first call on each device looks the array's device address up
+// with cudaGetSymbolAddress (the array's name in host code is only a host-side
+// stand-in, not a device address). Make that first call before capturing
+// any stream.
+#include "../../include/lbvh_gb300.h"
+
+#include "build.cuh"
+
+#include <mutex>
+
+using namespace lbvh_gb300;
+
+namespace {
+
+constexpr size_t kNoAllocMaxPrims = LBVH_NOALLOC_MAX_PRIMS;
+constexpr size_t kAlign = 256;
+
+constexpr size_t
+round_up(size_t x)
+{
+  return (x + kAlign - 1) / kAlign * kAlign;
+}
+
+constexpr size_t kTiles = (kNoAllocMaxPrims + kSortTile - 1) / kSortTile;
+constexpr size_t kBoundsBlocksMax = (kNoAllocMaxPrims + kBoundsThreads * 8 - 1) / (kBoundsThreads * 8);
+// scratch layout (byte offsets)
+constexpr size_t kOffState = 0;
+constexpr size_t kOffPartials = kOffState + round_up(sizeof(BuildState));
+constexpr size_t kOffKeysA = kOffPartials + round_up(kBoundsBlocksMax * 48);
+constexpr size_t kOffKeysB = kOffKeysA + round_up(4 * kNoAllocMaxPrims);
+constexpr size_t kOffLookback = kOffKeysB + round_up(4 * kNoAllocMaxPrims);
+constexpr size_t kOffChild = kOffLookback + round_up(kTiles * 256 * 8);
+constexpr size_t kOffLeafParent = kOffChild + round_up(8 * kNoAllocMaxPrims);
+constexpr size_t kOffNodeParent = kOffLeafParent + round_up(4 * kNoAllocMaxPrims);
+constexpr size_t kOffFlags = kOffNodeParent + round_up(4 * kNoAllocMaxPrims);
+constexpr size_t kScratchBytes = kOffFlags + round_up(4 * kNoAllocMaxPrims);
+
+// The scratch memory of every allocation-free build on this device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+
+struct DeviceSlot
+{
+  std::once_flag once;
+  cudaError_t setup_error = cudaSuccess;
+  unsigned char* scratch = nullptr; // device address of g_noalloc_scratch
+  int num_sms = 1;
+  uint32_t epoch = 0;               // look-back epoch of the last call
+};
+
+DeviceSlot g_slots[kMaxDevices];
+std::mutex g_epoch_mutex;
+
+bool
+is_device_pointer(const void* p, int device)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) &&
+         (a.type == cudaMemoryTypeManaged || a.device == device);
+}
+
+} // namespace
+
+extern "C" int
+lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint32_t* d_status, void* stream)
+{
+  if (!d_tris || !d_nodes)
+    return LBVH_ERR_INVALID_ARG;
+  if (n < 2 || n > kNoAllocMaxPrims)
+    return LBVH_ERR_INVALID_ARG; // beyond the fixed scratch: use lbvh_build_triangles
+  if ((reinterpret_cast<uintptr_t>(d_tris) & 15) || (reinterpret_cast<uintptr_t>(d_nodes) & 31))
+    return LBVH_ERR_INVALID_ARG;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) {
+    cudaGetLastError();
+    return LBVH_ERR_DEVICE;
+  }
+  if (!is_device_pointer(d_tris, device) || !is_device_pointer(d_nodes, device) ||
+      (d_status && !is_device_pointer(d_status, device)))
+    return LBVH_ERR_INVALID_ARG; // host memory would need staging buffers
+
+  DeviceSlot& slot = g_slots[device];
+  std::call_once(slot.once, [&slot, device]() {
+    // runs with `device` current (the caller's current device)
+    void* p = nullptr;
+    slot.setup_error = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (slot.setup_error == cudaSuccess) {
+      slot.scratch = static_cast<unsigned char*>(p);
+      slot.setup_error = cudaDeviceGetAttribute(&slot.num_sms, cudaDevAttrMultiProcessorCount, device);
+    }
+    if (slot.setup_error != cudaSuccess)
+      cudaGetLastError();
+  });
+  if (slot.setup_error != cudaSuccess || !slot.scratch)
+    return LBVH_ERR_DEVICE;
+
+  uint32_t epoch;
+  {
+    std::lock_guard<std::mutex> lock(g_epoch_mutex);
+    if (slot.epoch == 0 || slot.epoch > 0xfffffff0u)
+      slot.epoch = 4; // a wrapped counter would meet stale words: cleared below
+    epoch = slot.epoch;
+    slot.epoch += 4;
+  }
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned char* base = slot.scratch;
+  const uint32_t nn = uint32_t(n);
+  BuildBuffers b{};
+  b.state = reinterpret_cast<BuildState*>(base + kOffState);
+  b.partials = base + kOffPartials;
+  b.keys_a = reinterpret_cast<uint32_t*>(base + kOffKeysA);
+  b.keys_b = reinterpret_cast<uint32_t*>(base + kOffKeysB);
+  b.vals_a = nullptr; // parity build: key-only sort
+  b.vals_b = nullptr;
+  b.lookback = reinterpret_cast<unsigned long long*>(base + kOffLookback);
+  b.child = reinterpret_cast<uint2*>(base + kOffChild);
+  b.leaf_parent = reinterpret_cast<uint32_t*>(base + kOffLeafParent);
+  b.node_parent = reinterpret_cast<uint32_t*>(base + kOffNodeParent);
+  b.flags = reinterpret_cast<uint32_t*>(base + kOffFlags);
+  const uint32_t want = (nn + kBoundsThreads * 8 - 1) / (kBoundsThreads * 8);
+  const uint32_t cap = uint32_t(slot.num_sms) * 4;
+  b.bounds_blocks = want < 1 ? 1 : (want > cap ? cap : want);
+  const uint32_t mwant = (nn + kMortonThreads - 1) / kMortonThreads;
+  const uint32_t mcap = uint32_t(slot.num_sms) * 8;
+  b.morton_blocks = mwant < 1 ? 1 : (mwant > mcap ? mcap : mwant);
+
+  // What must start at zero: the bounds/sort counters and the error word,
+  // and the arrival flags (an earlier call that failed can leave them odd).
+  cudaError_t e = cudaMemsetAsync(b.state, 0, sizeof(BuildState), s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b.flags, 0, 4 * (n - 1), s);
+  if (e == cudaSuccess && epoch == 4)
+    e = cudaMemsetAsync(b.lookback, 0, kTiles * 256 * 8, s);
+  if (e == cudaSuccess)
+    e = launch_curve_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, s);
+  if (e == cudaSuccess)
+    e = launch_sort(nn, false, epoch, b, s);
+  if (e == cudaSuccess)
+    e = launch_fit_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, static_cast<Node*>(d_nodes), s);
+  if (e == cudaSuccess && d_status)
+    e = cudaMemcpyAsync(d_status, &b.state->error, 4, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return LBVH_ERR_DEVICE;
+  }
+  return LBVH_OK;
+}

@@ -1,0 +1,63 @@
+"""The allocation-free build entry point, called through the C ABI.
+
+lbvh_build_triangles_noalloc serves callers that cannot allocate device
+memory where they build a BVH (a frame loop that sizes everything at start-up,
+a plugin inside a host application that owns the GPU memory budget, a process
+whose memory another allocator holds). It keeps its scratch in one fixed array
+inside the library. This file is collected last, so a run that stops at the
+first failure has already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import lbvh_gb300 as lb
+from lbvh_gb300 import _lib, scenes
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _noalloc(tris, nodes, status, stream):
+    L = _lib.lib()
+    return L.lbvh_build_triangles_noalloc(
+        ctypes.c_void_p(tris.data_ptr()), tris.shape[0],
+        ctypes.c_void_p(nodes.data_ptr()),
+        ctypes.c_void_p(status.data_ptr()) if status is not None else None,
+        ctypes.c_void_p(stream))
+
+
+def test_noalloc_build_matches_allocating_build(lib_built):
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    ctx = lb.Context(0, stream)
+    status = torch.full((1,), 0xFFFF, dtype=torch.int32, device=dev)
+    # two calls in a row with different sizes: the second reuses (and must
+    # fully reset) the scratch the first one left behind
+    for n, seed in [(_lib.NOALLOC_MAX_PRIMS, 71), (3_001, 72), (2, 73)]:
+        tris = torch.from_numpy(scenes.soup(n, seed)).to(dev)
+        nodes = torch.empty(((n - 1) * 8,), dtype=torch.int32, device=dev)
+        status.fill_(0xFFFF)
+        assert _noalloc(tris, nodes, status, stream) == _lib.LBVH_OK
+        torch.cuda.synchronize()
+        assert int(status.item()) == 0
+        want = lb.Builder(ctx)(tris).nodes()  # the allocating entry point
+        got = nodes.cpu().numpy().view(lb.NODE_DTYPE)
+        assert got.tobytes() == want.tobytes(), n  # build parity is bit-exact
+
+
+def test_noalloc_rejects_what_it_cannot_serve(lib_built):
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    n = _lib.NOALLOC_MAX_PRIMS + 1
+    tris = torch.zeros((n, 12), dtype=torch.float32, device=dev)
+    nodes = torch.empty(((n - 1) * 8,), dtype=torch.int32, device=dev)
+    assert _noalloc(tris, nodes, None, stream) == _lib.LBVH_ERR_INVALID_ARG
+    one = torch.zeros((1, 12), dtype=torch.float32, device=dev)
+    assert _noalloc(one, nodes, None, stream) == _lib.LBVH_ERR_INVALID_ARG
+    host = torch.zeros((16, 12), dtype=torch.float32)
+    assert _noalloc(host, nodes, None, stream) == _lib.LBVH_ERR_INVALID_ARG
+    torch.cuda.synchronize()
