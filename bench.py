@@ -164,6 +164,41 @@ def run_reference(args, world, rank):
     return 0
 
 
+def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_kind, n=N_BUILD_16M):
+    """Device-resident build of the 16M-triangle random soup, L2 flushed
+    between builds; the HBM roofline workload."""
+    import torch
+
+    import lbvh_gb300 as lb
+    from lbvh_gb300 import scenes
+
+    soup = torch.from_numpy(scenes.soup_large(n, seed=16)).to(dev)
+    big = lb.BVH(ctx)
+    ctx.reserve(n, 0)
+    for _ in range(3):
+        builder(soup, into=big)
+    torch.cuda.synchronize()
+    bt = []
+    for _ in range(max(5, min(steps, 20))):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        builder(soup, into=big)
+        b.record(stream)
+        torch.cuda.synchronize()
+        bt.append(a.elapsed_time(b))
+    ctx.synchronize()
+    ms16 = float(np.mean(bt))
+    algo = n * sum(BYTES_PER_PRIM.values())
+    achieved = algo / (ms16 * 1e-3) / 1e9
+    return {"triangles": n, "ms": round(ms16, 4),
+            "mprims_s": round(n / (ms16 * 1e-3) / 1e6, 1),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                         "bytes_per_prim": sum(BYTES_PER_PRIM.values()),
+                         "traffic": None, "peak_kind": peak_kind}}
+
+
 # --------------------------------------------------------------------------
 # our arm
 
@@ -175,6 +210,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-16m", action="store_true", help="skip the 16M-triangle build measurement")
+    ap.add_argument("--only-16m", action="store_true", help="only the 16M-triangle build (profiling)")
+    ap.add_argument("--soup-n", type=int, default=N_BUILD_16M, help="soup size of the build measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -197,6 +234,14 @@ def main():
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     ctx = lb.Context(local, stream.cuda_stream)
+
+    if args.only_16m:
+        flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+        r = measure_build_16m(ctx, lb.Builder(ctx), stream, flush, dev, args.steps, hbm_peak, peak_kind,
+                              args.soup_n)
+        if rank == 0:
+            print(json.dumps({"build_16m": r}), flush=True)
+        return 0
 
     tris_h = scenes.torus_scene(seed=11)
     rays_h = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(tris_h, 1 << 20, 3)])
@@ -251,7 +296,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_ms = float(t.item())
     value = world * m / (step_ms * 1e-3) / 1e6
-    gpu_launches = args.steps * (8 + 1)  # bounds, Morton, 4 sort passes, split, fit; trace
+    gpu_launches = args.steps * (8 + 2)  # bounds, Morton, 4 sort passes, split, fit; repack, trace
 
     # correctness guard on the timed output: the same hits as an untimed run
     ref_hits = torch.empty_like(hits)
@@ -289,36 +334,12 @@ def main():
                 "traffic": None, "peak_kind": peak_kind,
                 "note": "traversal is latency/issue bound; see build_16m for the HBM-bound build"}
 
-    # ---- 16M-triangle build (roofline workload), per stage ----------------
+    # ---- 16M-triangle build (roofline workload) ----------------------------
     build_16m = None
     if not args.no_16m:
         del tris_p, rays_p, hits_p
-        soup = torch.from_numpy(scenes.soup_large(N_BUILD_16M, seed=16)).to(dev)
-        big = lb.BVH(ctx)
-        ctx.reserve(N_BUILD_16M, 0)
-        for _ in range(3):
-            builder(soup, into=big)
-        torch.cuda.synchronize()
-        bt = []
-        for _ in range(max(5, min(args.steps, 20))):
-            flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            builder(soup, into=big)
-            b.record(stream)
-            torch.cuda.synchronize()
-            bt.append(a.elapsed_time(b))
-        ms16 = float(np.mean(bt))
-        algo = N_BUILD_16M * sum(BYTES_PER_PRIM.values())
-        achieved = algo / (ms16 * 1e-3) / 1e9
-        build_16m = {"triangles": N_BUILD_16M, "ms": round(ms16, 4),
-                     "mprims_s": round(N_BUILD_16M / (ms16 * 1e-3) / 1e6, 1),
-                     "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
-                                  "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                                  "bytes_per_prim": sum(BYTES_PER_PRIM.values()),
-                                  "traffic": None, "peak_kind": peak_kind}}
-        ctx.synchronize()
-        del soup, big
+        build_16m = measure_build_16m(ctx, builder, stream, flush, dev, args.steps, hbm_peak, peak_kind,
+                                      args.soup_n)
 
     # ---- CPU baseline: the oracle port (or reference) on the host cores ---
     cpu = None

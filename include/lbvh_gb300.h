@@ -114,6 +114,12 @@ LBVH_API const char* lbvh_ctx_last_error(const lbvh_ctx* ctx);
  * traces of up to n_rays host-side rays, so later calls allocate nothing. */
 LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 
+/* Launch-shape parameters (lbvh_ctx_set_param). No reference counterpart:
+ * they tune the GPU kernels, not the results. */
+#define LBVH_PARAM_TRACE_BLOCKS_PER_SM 1 /* persistent traversal grid, 1..32 */
+#define LBVH_PARAM_TRACE_REFILL 2        /* idle lanes before a warp refills, 1..32 */
+LBVH_API int lbvh_ctx_set_param(lbvh_ctx* ctx, int param, int value);
+
 /* Replaces the reference triangle constructor triangle<float>(a, b, c)
  * (lbvh.h:1967-1972) for n triangles: verts is n x 9 float32 (a, b, c),
  * tris_out is n x 12 float32. Bit-identical to the reference compiled

@@ -21,6 +21,8 @@ LBVH_ERR_DEVICE = 4
 LBVH_ERR_BAD_TOPOLOGY = 5
 
 NOALLOC_MAX_PRIMS = 65536
+PARAM_TRACE_BLOCKS_PER_SM = 1
+PARAM_TRACE_REFILL = 2
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000
@@ -41,6 +43,7 @@ SIGNATURES = {
     "lbvh_ctx_synchronize": (_I, [_P]),
     "lbvh_ctx_last_error": (ctypes.c_char_p, [_P]),
     "lbvh_ctx_reserve": (_I, [_P, _S, _S]),
+    "lbvh_ctx_set_param": (_I, [_P, _I, _I]),
     "lbvh_make_triangles": (_I, [_P, _P, _S, _P]),
     "lbvh_bvh_create": (_I, [_P, _PP]),
     "lbvh_bvh_destroy": (_I, [_P, _P]),

@@ -112,6 +112,9 @@ class Context:
     def synchronize(self):
         self.check(_lib.lib().lbvh_ctx_synchronize(self._h))
 
+    def set_param(self, param: int, value: int):
+        self.check(_lib.lib().lbvh_ctx_set_param(self._h, param, value))
+
     def reserve(self, n_prims: int, n_rays: int = 0):
         self.check(_lib.lib().lbvh_ctx_reserve(self._h, n_prims, n_rays))
 

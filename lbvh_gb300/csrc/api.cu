@@ -45,6 +45,8 @@ struct lbvh_ctx
   DevBuf hits;                 // staging for host hits
   DevBuf counts;               // staging for host per-ray counts
   DevBuf prims_in;             // staging for host refit input
+  uint32_t* ray_counter = nullptr; // persistent-trace ray dispenser
+  TraceParams trace;               // traversal launch shape
   uint32_t epoch = 0;          // look-back epoch of the last sort pass
   char msg[512] = { 0 };
 };
@@ -61,6 +63,8 @@ struct lbvh_bvh
   DevBuf sorted_prims;         // sorted-leaf mode: primitives in leaf order
   DevBuf leaf_prim;            // sorted-leaf mode: leaf slot -> primitive id
   DevBuf curve;                // keep-curve: codes, sorted codes, perm, bounds
+  DevBuf wnodes;               // traversal copy (WideNode per internal node)
+  bool wnodes_valid = false;   // false after every build / refit
 };
 
 namespace {
@@ -329,6 +333,7 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
   bvh->n = nn;
   bvh->flags = flags;
   bvh->kind = kind;
+  bvh->wnodes_valid = false;
   bvh->prims = dprims;
   bvh->device = c->device;
   if (!on_device(prims))
@@ -375,6 +380,7 @@ refit_common(lbvh_ctx* c, lbvh_bvh* bvh, const float* prims, int kind)
     CK(launch_refit_boxes(static_cast<const Box*>(dprims), n, c->bufs, nodes, c->stream), "refit launch");
   }
   bvh->prims = dprims;
+  bvh->wnodes_valid = false;
   if (host)
     return check_device(c);
   return LBVH_OK;
@@ -426,6 +432,8 @@ lbvh_ctx_create(int device, void* stream, lbvh_ctx** out)
     cudaGetLastError();
     if (c->h_err)
       cudaFreeHost(c->h_err);
+    if (c->ray_counter)
+      cudaFree(c->ray_counter);
     if (c->state)
       cudaFree(c->state);
     delete c;
@@ -442,6 +450,8 @@ lbvh_ctx_create(int device, void* stream, lbvh_ctx** out)
   if ((e = cudaMemset(c->state, 0, sizeof(BuildState))) != cudaSuccess)
     return bail(e);
   if ((e = cudaMallocHost(&c->h_err, 64)) != cudaSuccess)
+    return bail(e);
+  if ((e = cudaMalloc(&c->ray_counter, 256)) != cudaSuccess)
     return bail(e);
   *out = c;
   return LBVH_OK;
@@ -463,6 +473,7 @@ lbvh_ctx_destroy(lbvh_ctx* c)
   release(c->prims_in, c->stream);
   cudaStreamSynchronize(c->stream);
   cudaFree(c->state);
+  cudaFree(c->ray_counter);
   cudaFreeHost(c->h_err);
   delete c;
   return LBVH_OK;
@@ -500,6 +511,27 @@ lbvh_ctx_reserve(lbvh_ctx* c, size_t n_prims, size_t n_rays)
     CK(reserve(c->hits, 16 * n_rays, c->stream), "hit staging allocation");
   }
   return LBVH_OK;
+}
+
+int
+lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
+{
+  if (!c)
+    return LBVH_ERR_INVALID_ARG;
+  switch (param) {
+    case LBVH_PARAM_TRACE_BLOCKS_PER_SM:
+      if (value < 1 || value > 32)
+        return fail(c, LBVH_ERR_INVALID_ARG, "trace blocks per SM %d outside [1, 32]", value);
+      c->trace.blocks_per_sm = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_TRACE_REFILL:
+      if (value < 1 || value > 32)
+        return fail(c, LBVH_ERR_INVALID_ARG, "refill threshold %d outside [1, 32]", value);
+      c->trace.refill = uint32_t(value);
+      return LBVH_OK;
+    default:
+      return fail(c, LBVH_ERR_INVALID_ARG, "unknown parameter %d", param);
+  }
 }
 
 int
@@ -559,6 +591,7 @@ lbvh_bvh_destroy(lbvh_ctx* c, lbvh_bvh* b)
   release(b->sorted_prims, c->stream);
   release(b->leaf_prim, c->stream);
   release(b->curve, c->stream);
+  release(b->wnodes, c->stream);
   delete b;
   return LBVH_OK;
 }
@@ -654,7 +687,7 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
     return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
   if (b->n < 2 || b->kind != kKindTris)
     return fail(c, LBVH_ERR_INVALID_ARG, "BVH was not built from triangles");
-  if (m > 0xffffffffull)
+  if (m > 0x7fffffffull)
     return fail(c, LBVH_ERR_INVALID_ARG, "ray count %zu too large", m);
   if (m == 0)
     return LBVH_OK;
@@ -690,8 +723,17 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
                                                           : static_cast<const Tri*>(b->prims);
   const uint32_t* leaf_prim =
     (b->flags & LBVH_BUILD_SORTED_LEAVES) ? static_cast<const uint32_t*>(b->leaf_prim.ptr) : nullptr;
-  CK(launch_trace_tris(static_cast<const Node*>(b->nodes.ptr), tris, leaf_prim, dr, uint32_t(m), dh,
-                       counts ? db : nullptr, counts ? dt : nullptr, c->stream),
+  lbvh_bvh* mb = const_cast<lbvh_bvh*>(b); // the traversal copy is a cache
+  if (!mb->wnodes_valid) {
+    CK(reserve(mb->wnodes, sizeof(WideNode) * b->n, c->stream), "traversal layout allocation");
+    CK(launch_repack(static_cast<const Node*>(b->nodes.ptr), b->n - 1, static_cast<WideNode*>(mb->wnodes.ptr),
+                     c->stream),
+       "repack launch");
+    mb->wnodes_valid = true;
+  }
+  CK(launch_trace_tris(static_cast<const WideNode*>(b->wnodes.ptr), b->n - 1, tris, leaf_prim, dr, uint32_t(m), dh,
+                       counts ? db : nullptr, counts ? dt : nullptr, c->ray_counter, c->num_sms, c->trace,
+                       c->stream),
      "trace launch");
   if (hh)
     CK(cudaMemcpyAsync(hits, dh, 16 * m, cudaMemcpyDeviceToHost, c->stream), "hit download");

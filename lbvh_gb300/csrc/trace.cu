@@ -1,8 +1,8 @@
 // Closest-hit ray/triangle traversal for sm_103a.
 //
 // Replaces traverser<float, triangle<float>, triangle_intersection<float>>::
-// operator() with triangle_intersector<float> (lbvh.h:1869-1942, 2055-2075),
-// one ray per thread, with the reference's exact visiting order:
+// operator() with triangle_intersector<float> (lbvh.h:1869-1942, 2055-2075)
+// with the reference's exact visiting order, per ray:
 //   * a 128-entry stack of {node, tmin} that drops pushes when full
 //     (lbvh.h:1746-1789), seeded with {root, +inf};
 //   * pop; skip if closest.t < entry.tmin;
@@ -11,6 +11,15 @@
 //   * both hit: push the farther first (equal tmin: right popped first).
 // All arithmetic uses explicit round-to-nearest ops, so hits (id, t, u, v)
 // are bit-identical to the reference.
+//
+// GB300 mapping:
+//   * a traversal copy of the tree in which each internal node carries both
+//     children's boxes (64 bytes, four 16-byte loads from one line), built
+//     once per build by k_repack;
+//   * persistent warps: a lane whose ray has finished takes the next ray of
+//     its warp's batch (ballot + shuffle), and a warp fetches a new batch of
+//     32 rays with one atomic, so lanes do not idle while the longest ray of
+//     a fixed group finishes.
 #include "trace.cuh"
 
 namespace lbvh_gb300 {
@@ -21,6 +30,7 @@ struct RayCtx
   float rx, ry, rz;   // reciprocal direction
   float ix, iy, iz;   // (-pos) * rcp
   bool sx, sy, sz;    // dir > 0: near plane is the box minimum
+  bool fast;          // no slab value can be NaN: min/max may use fminf/fmaxf
 };
 
 __device__ __forceinline__ RayCtx
@@ -45,21 +55,35 @@ make_ray(const float4 a, const float4 b)
   r.sx = r.dx > 0.0f;
   r.sy = r.dy > 0.0f;
   r.sz = r.dz > 0.0f;
+  // |dir| >= 2^-60 and |pos| <= 2^60 (false for NaN), with every box
+  // coordinate within 2^60 (checked by k_repack), bound |b * rcp| and
+  // |pos * rcp| by 2^120: every slab value is finite.
+  const float lo = 0x1p-60f, hi = 0x1p60f;
+  r.fast = fabsf(r.dx) >= lo && fabsf(r.dy) >= lo && fabsf(r.dz) >= lo && fabsf(r.px) <= hi &&
+           fabsf(r.py) <= hi && fabsf(r.pz) <= hi;
   return r;
 }
 
 // detail::intersect (octant form) + box_intersection::operator bool,
-// lbvh.h:1026-1029, 1071-1091. Box = {lo.x, lo.y, lo.z, hi.x}, {hi.y, hi.z}.
+// lbvh.h:1026-1029, 1071-1091.
 __device__ __forceinline__ bool
-box_test(const RayCtx& r, float4 a, float2 b, float& tmin_out)
+box_test(const RayCtx& r, float lox, float loy, float loz, float hix, float hiy, float hiz, float& tmin_out)
 {
-  const float lox = a.x, loy = a.y, loz = a.z, hix = a.w, hiy = b.x, hiz = b.y;
   const float tn0 = fadd(fmul(r.sx ? lox : hix, r.rx), r.ix);
   const float tn1 = fadd(fmul(r.sy ? loy : hiy, r.ry), r.iy);
   const float tn2 = fadd(fmul(r.sz ? loz : hiz, r.rz), r.iz);
   const float tf0 = fadd(fmul(r.sx ? hix : lox, r.rx), r.ix);
   const float tf1 = fadd(fmul(r.sy ? hiy : loy, r.ry), r.iy);
   const float tf2 = fadd(fmul(r.sz ? hiz : loz, r.rz), r.iz);
+  if (r.fast) {
+    // Finite operands: fmaxf/fminf pick the same value as the reference's
+    // ternaries, up to the sign of a zero, and every later use of tmin/tmax
+    // is a comparison, which ignores that sign.
+    const float tmin = fmaxf(fmaxf(tn0, tn1), tn2);
+    const float tmax = fminf(fminf(tf0, tf1), tf2);
+    tmin_out = tmin;
+    return tmax >= fmaxf(0.0f, tmin);
+  }
   const float tmin = mmax(mmax(tn0, tn1), tn2);
   const float tmax = mmin(mmin(tf0, tf1), tf2);
   tmin_out = tmin;
@@ -91,106 +115,231 @@ tri_test(const RayCtx& r, const Tri* __restrict__ tris, uint32_t p, float& t, fl
   return false;
 }
 
-template<bool kCounts>
-__global__ __launch_bounds__(kTraceThreads) void
-k_trace_tris(const Node* __restrict__ nodes,
-             const Tri* __restrict__ tris,
-             const uint32_t* __restrict__ leaf_prim,
-             const float4* __restrict__ rays,
-             uint32_t m,
-             Hit* __restrict__ hits,
-             uint32_t* __restrict__ n_box,
-             uint32_t* __restrict__ n_tri)
+// ---------------------------------------------------------------------------
+// Traversal layout: node i = {left box, right box, left, right} in 64 bytes.
+// A leaf child's box slot is unused (the reference tests leaf triangles
+// directly).
+
+__device__ __forceinline__ bool
+bounded(float4 v)
+{
+  const float hi = 0x1p60f; // false for NaN
+  return fabsf(v.x) <= hi && fabsf(v.y) <= hi && fabsf(v.z) <= hi && fabsf(v.w) <= hi;
+}
+
+__global__ void
+k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict__ out, uint32_t* __restrict__ wide)
 {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m)
+  if (i >= n_nodes)
     return;
-  const RayCtx r = make_ray(__ldg(rays + 2 * size_t(i)), __ldg(rays + 2 * size_t(i) + 1));
+  const float4* nv = reinterpret_cast<const float4*>(nodes);
+  const float4 self = __ldg(nv + 2 * size_t(i) + 1);
+  const uint32_t l = __float_as_uint(self.z), r = __float_as_uint(self.w);
+  float4 la = make_float4(0, 0, 0, 0), lb = la, ra = la, rb = la;
+  if (!(l & kLeafBit) && l < n_nodes) {
+    la = __ldg(nv + 2 * size_t(l));
+    lb = __ldg(nv + 2 * size_t(l) + 1);
+  }
+  if (!(r & kLeafBit) && r < n_nodes) {
+    ra = __ldg(nv + 2 * size_t(r));
+    rb = __ldg(nv + 2 * size_t(r) + 1);
+  }
+  if (!bounded(la) || !bounded(make_float4(lb.x, lb.y, ra.x, ra.y)) || !bounded(make_float4(ra.z, ra.w, rb.x, rb.y)))
+    atomicOr(wide, 1u); // a coordinate beyond 2^60: no fast slab path
+  WideNode w;
+  w.a = make_float4(la.x, la.y, la.z, la.w); // left lo.xyz, hi.x
+  w.b = make_float4(lb.x, lb.y, ra.x, ra.y); // left hi.yz, right lo.xy
+  w.c = make_float4(ra.z, ra.w, rb.x, rb.y); // right lo.z, hi.xyz
+  w.d = make_float4(__uint_as_float(l), __uint_as_float(r), 0.0f, 0.0f);
+  out[i] = w;
+}
+
+// ---------------------------------------------------------------------------
+
+template<bool kCounts>
+__global__ __launch_bounds__(kTraceThreads) void
+k_trace(const WideNode* __restrict__ wnodes,
+        const Tri* __restrict__ tris,
+        const uint32_t* __restrict__ leaf_prim,
+        const float4* __restrict__ rays,
+        uint32_t m,
+        Hit* __restrict__ hits,
+        uint32_t* __restrict__ n_box,
+        uint32_t* __restrict__ n_tri,
+        uint32_t* __restrict__ ray_counter,
+        const uint32_t* __restrict__ wide,
+        uint32_t refill)
+{
+  const bool scene_fast = __ldg(wide) == 0;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
   const float inf = __int_as_float(0x7f800000);
 
+  // The traversal stack: entries [0, sp) in local memory plus, when has_cur,
+  // one more entry on top held in registers (the entry popped next). The
+  // 128-entry capacity applies to the whole, so pushes drop exactly when the
+  // reference's would.
   uint2 stack[kStackSize];
   uint32_t sp = 0;
-  stack[sp++] = make_uint2(0u, __float_as_uint(inf));
-
+  uint2 cur = make_uint2(0u, 0u);
+  bool has_cur = false;
+  uint32_t ray = kMiss; // ray index of this lane, kMiss = none
+  RayCtx r{};
   uint32_t best_p = kMiss;
   float best_t = inf, best_u = 0.0f, best_v = 0.0f;
   uint32_t cb = 0, ct = 0;
 
-  const float4* nv = reinterpret_cast<const float4*>(nodes);
-  while (sp) {
-    const uint2 e = stack[--sp];
-    if (best_t < __uint_as_float(e.y))
+  // the warp's current batch of 32 ray ids (warp-uniform state)
+  uint32_t batch = 0, batch_left = 0;
+  bool no_more = false; // the last batch fetched reached the end of the rays
+
+  for (;;) {
+    // ---- refill idle lanes from the warp's batch (ballot + shuffle) ----
+    const uint32_t idle = __ballot_sync(0xffffffffu, ray == kMiss);
+    if (__popc(idle) >= refill) { // warp-uniform; refill <= 32
+      const uint32_t next_id = batch + 32 - batch_left;
+      const bool more = (batch_left > 0 && next_id < m) || !no_more;
+      if (!more) {
+        if (idle == 0xffffffffu)
+          break; // every ray handed to this warp has finished
+      } else {
+        const uint32_t want = __popc(idle);
+        const uint32_t got = min(want, batch_left);
+        batch_left -= got;
+        uint32_t extra_base = 0;
+        bool fetched = false;
+        if (got < want && !no_more) {
+          uint32_t nb = 0;
+          if (lane == 0)
+            nb = atomicAdd(ray_counter, 32u);
+          nb = __shfl_sync(0xffffffffu, nb, 0);
+          no_more = nb + 32 >= m;
+          extra_base = nb;
+          batch = nb;
+          batch_left = 32 - (want - got);
+          fetched = true;
+        }
+        if (ray == kMiss) {
+          const uint32_t k = __popc(idle & lt_mask);
+          uint32_t id = kMiss;
+          if (k < got)
+            id = next_id + k;
+          else if (fetched)
+            id = extra_base + (k - got);
+          if (id < m) {
+            ray = id;
+            r = make_ray(__ldg(rays + 2 * size_t(id)), __ldg(rays + 2 * size_t(id) + 1));
+            r.fast = r.fast && scene_fast;
+            sp = 0;
+            cur = make_uint2(0u, __float_as_uint(inf)); // root, pushed with +inf
+            has_cur = true;
+            best_p = kMiss;
+            best_t = inf;
+            best_u = best_v = 0.0f;
+            cb = ct = 0;
+          }
+        }
+      }
+    }
+    if (ray == kMiss)
       continue;
-    const float4 nb = __ldg(nv + 2 * size_t(e.x) + 1);
-    const uint32_t left = __float_as_uint(nb.z), right = __float_as_uint(nb.w);
-    bool lhit = false, rhit = false;
-    float lt = inf, rt = inf;
-    if (left & kLeafBit) {
-      const uint32_t p = left & ~kLeafBit;
-      float t, u, v;
-      if (kCounts)
-        ct++;
-      if (tri_test(r, tris, p, t, u, v) && t < best_t) {
-        best_p = p;
-        best_t = t;
-        best_u = u;
-        best_v = v;
+
+    // ---- one node visit (lbvh.h:1902-1938); cur passed the cull test ----
+    {
+      const float4* w = reinterpret_cast<const float4*>(wnodes + cur.x);
+      const float4 A = __ldg(w + 0), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+      const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
+      bool lhit = false, rhit = false;
+      float lt = inf, rt = inf;
+      if (!(left & kLeafBit)) {
+        if (kCounts)
+          cb++;
+        lhit = box_test(r, A.x, A.y, A.z, A.w, B.x, B.y, lt);
       }
-    } else {
-      if (kCounts)
-        cb++;
-      const float4 a = __ldg(nv + 2 * size_t(left));
-      const float2 b = __ldg(reinterpret_cast<const float2*>(nv + 2 * size_t(left) + 1));
-      lhit = box_test(r, a, b, lt);
-    }
-    if (right & kLeafBit) {
-      const uint32_t p = right & ~kLeafBit;
-      float t, u, v;
-      if (kCounts)
-        ct++;
-      if (tri_test(r, tris, p, t, u, v) && t < best_t) {
-        best_p = p;
-        best_t = t;
-        best_u = u;
-        best_v = v;
+      if (!(right & kLeafBit)) {
+        if (kCounts)
+          cb++;
+        rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
       }
-    } else {
-      if (kCounts)
-        cb++;
-      const float4 a = __ldg(nv + 2 * size_t(right));
-      const float2 b = __ldg(reinterpret_cast<const float2*>(nv + 2 * size_t(right) + 1));
-      rhit = box_test(r, a, b, rt);
+      // leaf triangles, left before right (equal t: the first tested wins)
+#pragma unroll 1
+      for (int k = 0; k < 2; k++) {
+        const uint32_t c = k == 0 ? left : right;
+        if (c & kLeafBit) {
+          const uint32_t p = c & ~kLeafBit;
+          float t, u, v;
+          if (kCounts)
+            ct++;
+          if (tri_test(r, tris, p, t, u, v) && t < best_t) {
+            best_p = p;
+            best_t = t;
+            best_u = u;
+            best_v = v;
+          }
+        }
+      }
+      // pushes; the last one pushed stays in registers as the next pop
+      has_cur = false;
+      if (lhit && rhit) {
+        const bool lfirst = lt < rt; // left nearer: push right, then left
+        const uint2 far = lfirst ? make_uint2(right, __float_as_uint(rt)) : make_uint2(left, __float_as_uint(lt));
+        const uint2 near = lfirst ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
+        if (sp < kStackSize)
+          stack[sp++] = far;
+        if (sp < kStackSize) {
+          cur = near;
+          has_cur = true;
+        }
+      } else if (lhit || rhit) {
+        if (sp < kStackSize) {
+          cur = lhit ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
+          has_cur = true;
+        }
+      }
     }
-    if (lhit && rhit) {
-      const bool lfirst = lt < rt; // left nearer: push right, then left
-      const uint2 fst = lfirst ? make_uint2(right, __float_as_uint(rt)) : make_uint2(left, __float_as_uint(lt));
-      const uint2 snd = lfirst ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
-      if (sp < kStackSize)
-        stack[sp++] = fst;
-      if (sp < kStackSize)
-        stack[sp++] = snd;
-    } else if (lhit) {
-      if (sp < kStackSize)
-        stack[sp++] = make_uint2(left, __float_as_uint(lt));
-    } else if (rhit) {
-      if (sp < kStackSize)
-        stack[sp++] = make_uint2(right, __float_as_uint(rt));
+    // ---- next entry: pop until one passes the cull test (lbvh.h:1893-1900) ----
+    for (;;) {
+      if (!has_cur) {
+        if (sp == 0)
+          break;
+        cur = stack[--sp];
+      }
+      has_cur = !(best_t < __uint_as_float(cur.y));
+      if (has_cur)
+        break;
     }
-  }
-  Hit h;
-  h.prim = (best_p != kMiss && leaf_prim) ? __ldg(leaf_prim + best_p) : best_p;
-  h.t = best_t;
-  h.u = best_p != kMiss ? best_u : 0.0f;
-  h.v = best_p != kMiss ? best_v : 0.0f;
-  hits[i] = h;
-  if (kCounts) {
-    n_box[i] = cb;
-    n_tri[i] = ct;
+    if (!has_cur) {
+      Hit h;
+      h.prim = (best_p != kMiss && leaf_prim) ? __ldg(leaf_prim + best_p) : best_p;
+      h.t = best_t;
+      h.u = best_p != kMiss ? best_u : 0.0f;
+      h.v = best_p != kMiss ? best_v : 0.0f;
+      hits[ray] = h;
+      if (kCounts) {
+        n_box[ray] = cb;
+        n_tri[ray] = ct;
+      }
+      ray = kMiss;
+    }
   }
 }
 
 cudaError_t
-launch_trace_tris(const Node* nodes,
+launch_repack(const Node* nodes, uint32_t n_nodes, WideNode* out, cudaStream_t s)
+{
+  // the scene-bound flag lives in the word after the last node
+  uint32_t* wide = reinterpret_cast<uint32_t*>(out + n_nodes);
+  cudaError_t e = cudaMemsetAsync(wide, 0, 4, s);
+  if (e != cudaSuccess)
+    return e;
+  k_repack<<<ceil_div_u32(n_nodes, 256), 256, 0, s>>>(nodes, n_nodes, out, wide);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_trace_tris(const WideNode* wnodes,
+                  uint32_t n_nodes,
                   const Tri* tris,
                   const uint32_t* leaf_prim,
                   const float* rays,
@@ -198,16 +347,28 @@ launch_trace_tris(const Node* nodes,
                   Hit* hits,
                   uint32_t* n_box,
                   uint32_t* n_tri,
+                  uint32_t* ray_counter,
+                  int num_sms,
+                  const TraceParams& p,
                   cudaStream_t s)
 {
   if (m == 0)
     return cudaSuccess;
-  const uint32_t blocks = ceil_div_u32(m, kTraceThreads);
+  cudaError_t e = cudaMemsetAsync(ray_counter, 0, 4, s);
+  if (e != cudaSuccess)
+    return e;
+  // persistent grid: enough resident warps per SM, never more than the rays
+  const uint32_t want = ceil_div_u32(m, kTraceThreads);
+  const uint32_t cap = uint32_t(num_sms) * p.blocks_per_sm;
+  const uint32_t blocks = want < cap ? want : cap;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
+  const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + n_nodes);
   if (n_box && n_tri)
-    k_trace_tris<true><<<blocks, kTraceThreads, 0, s>>>(nodes, tris, leaf_prim, r4, m, hits, n_box, n_tri);
+    k_trace<true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri, ray_counter,
+                                                   wide, p.refill);
   else
-    k_trace_tris<false><<<blocks, kTraceThreads, 0, s>>>(nodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr);
+    k_trace<false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
+                                                    ray_counter, wide, p.refill);
   return cudaGetLastError();
 }
 

@@ -8,7 +8,28 @@ namespace lbvh_gb300 {
 constexpr int kTraceThreads = 128;
 constexpr uint32_t kStackSize = 128; // traversal_stack<scalar, 128>, lbvh.h:1874
 
-cudaError_t launch_trace_tris(const Node* nodes,
+// Launch shape of the persistent traversal kernel (set per context).
+struct TraceParams
+{
+  uint32_t blocks_per_sm = 8; // resident 128-thread blocks per SM
+  uint32_t refill = 12;       // idle lanes at which a warp takes new rays
+};
+
+// Traversal copy of an internal node: both children's boxes plus the child
+// references, 64 bytes.
+//   a = {left lo.xyz, left hi.x}, b = {left hi.yz, right lo.xy},
+//   c = {right lo.z, right hi.xyz}, d = {left, right, 0, 0}
+struct __align__(16) WideNode
+{
+  float4 a, b, c, d;
+};
+static_assert(sizeof(WideNode) == 64, "wide node layout");
+
+cudaError_t launch_repack(const Node* nodes, uint32_t n_nodes, WideNode* out, cudaStream_t s);
+
+// wnodes holds n_nodes nodes followed by the scene-bound flag word.
+cudaError_t launch_trace_tris(const WideNode* wnodes,
+                              uint32_t n_nodes,
                               const Tri* tris,
                               const uint32_t* leaf_prim,
                               const float* rays,
@@ -16,6 +37,9 @@ cudaError_t launch_trace_tris(const Node* nodes,
                               Hit* hits,
                               uint32_t* n_box,
                               uint32_t* n_tri,
+                              uint32_t* ray_counter,
+                              int num_sms,
+                              const TraceParams& p,
                               cudaStream_t s);
 
 } // namespace lbvh_gb300
