@@ -39,7 +39,7 @@ struct lbvh_ctx
   DevBuf ws;                   // build workspace arena
   size_t ws_prims = 0;         // primitives the arena is laid out for
   BuildBuffers bufs{};
-  DevBuf flags;                // arrival counters, even between builds
+  DevBuf slots;                // tree arrival slots (epoch-tagged, persistent)
   DevBuf lookback;             // radix sort look-back words (epoch-tagged)
   DevBuf rays;                 // staging for host rays
   DevBuf hits;                 // staging for host hits
@@ -182,6 +182,7 @@ ws_reserve(lbvh_ctx* c, size_t n)
   const size_t o_child = take(8 * n);
   const size_t o_lp = take(4 * n);
   const size_t o_np = take(4 * n);
+  const size_t o_pend = take(32 * size_t(kTreePendingPerBlock) * ((n + kTreeBlock - 1) / kTreeBlock));
   CK(reserve(c->ws, off, c->stream), "workspace allocation");
   // The look-back buffer only ever holds look-back words: fresh words read as
   // "not published" (epoch 0 is never used), so it is cleared only on growth.
@@ -189,10 +190,12 @@ ws_reserve(lbvh_ctx* c, size_t n)
   CK(reserve(c->lookback, tiles * 256 * 8, c->stream, &grew), "look-back allocation");
   if (grew)
     CK(cudaMemsetAsync(c->lookback.ptr, 0, c->lookback.cap, c->stream), "look-back clear");
-  if (c->flags.cap < 4 * n) {
-    CK(reserve(c->flags, 4 * n, c->stream), "flag allocation");
-    CK(cudaMemsetAsync(c->flags.ptr, 0, c->flags.cap, c->stream), "flag clear");
-  }
+  // Like the look-back words, slots carry the epoch of the build that wrote
+  // them, so they are cleared only when (re)allocated.
+  grew = false;
+  CK(reserve(c->slots, 8 * n, c->stream, &grew), "slot allocation");
+  if (grew)
+    CK(cudaMemsetAsync(c->slots.ptr, 0, c->slots.cap, c->stream), "slot clear");
   char* base = static_cast<char*>(c->ws.ptr);
   BuildBuffers& b = c->bufs;
   b.state = c->state;
@@ -205,19 +208,23 @@ ws_reserve(lbvh_ctx* c, size_t n)
   b.child = reinterpret_cast<uint2*>(base + o_child);
   b.leaf_parent = reinterpret_cast<uint32_t*>(base + o_lp);
   b.node_parent = reinterpret_cast<uint32_t*>(base + o_np);
-  b.flags = static_cast<uint32_t*>(c->flags.ptr);
+  b.pending = base + o_pend;
+  b.slots = static_cast<unsigned long long*>(c->slots.ptr);
   c->ws_prims = n;
   return LBVH_OK;
 }
 
-// Next look-back epoch base (4 passes per sort). Epoch 0 means "never
-// written"; on wrap-around the look-back words are cleared.
+// Next epoch base: the four sort passes use base .. base + 3 for their
+// look-back words, the tree build or refit uses base for its slots. Epoch 0
+// means "never written"; on wrap-around both buffers are cleared.
 int
 next_epoch(lbvh_ctx* c, uint32_t* base)
 {
   if (c->epoch == 0 || c->epoch > 0xfffffff0u) {
     if (c->epoch != 0 && c->lookback.ptr)
       CK(cudaMemsetAsync(c->lookback.ptr, 0, c->lookback.cap, c->stream), "look-back clear");
+    if (c->epoch != 0 && c->slots.ptr)
+      CK(cudaMemsetAsync(c->slots.ptr, 0, c->slots.cap, c->stream), "slot clear");
     c->epoch = 4;
   }
   *base = c->epoch;
@@ -235,15 +242,10 @@ check_device(lbvh_ctx* c)
   if (!err)
     return LBVH_OK;
   CK(cudaMemsetAsync(&c->state->error, 0, 4, c->stream), "status clear");
-  // an interrupted build can leave arrival flags odd: start them over
-  if (c->flags.ptr)
-    CK(cudaMemsetAsync(c->flags.ptr, 0, c->flags.cap, c->stream), "flag clear");
   CK(cudaMemsetAsync(c->state, 0, offsetof(BuildState, error), c->stream), "state clear");
   CK(cudaStreamSynchronize(c->stream), "stream synchronize");
   if (err & kErrLookbackTimeout)
     return fail(c, LBVH_ERR_TIMEOUT, "radix sort look-back wait expired");
-  if (err & kErrFitTimeout)
-    return fail(c, LBVH_ERR_TIMEOUT, "box fit wait expired");
   return fail(c, LBVH_ERR_BAD_TOPOLOGY, "node array is not a binary tree over its leaves");
 }
 
@@ -318,17 +320,17 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
     if (kind == kKindTris) {
       Tri* sp = static_cast<Tri*>(bvh->sorted_prims.ptr);
       CK(launch_gather_tris(static_cast<const Tri*>(dprims), b.vals_a, nn, sp, c->stream), "gather launch");
-      CK(launch_fit_tris(sp, nn, b, nodes, c->stream), "fit launch");
+      CK(launch_fit_tris(sp, nn, b, nodes, epoch, c->stream), "fit launch");
     } else {
       Box* sp = static_cast<Box*>(bvh->sorted_prims.ptr);
       CK(launch_gather_boxes(static_cast<const Box*>(dprims), b.vals_a, nn, sp, c->stream), "gather launch");
-      CK(launch_fit_boxes(sp, nn, b, nodes, c->stream), "fit launch");
+      CK(launch_fit_boxes(sp, nn, b, nodes, epoch, c->stream), "fit launch");
     }
   } else {
     if (kind == kKindTris)
-      CK(launch_fit_tris(static_cast<const Tri*>(dprims), nn, b, nodes, c->stream), "fit launch");
+      CK(launch_fit_tris(static_cast<const Tri*>(dprims), nn, b, nodes, epoch, c->stream), "fit launch");
     else
-      CK(launch_fit_boxes(static_cast<const Box*>(dprims), nn, b, nodes, c->stream), "fit launch");
+      CK(launch_fit_boxes(static_cast<const Box*>(dprims), nn, b, nodes, epoch, c->stream), "fit launch");
   }
   bvh->n = nn;
   bvh->flags = flags;
@@ -362,22 +364,25 @@ refit_common(lbvh_ctx* c, lbvh_bvh* bvh, const float* prims, int kind)
   }
   if ((st = ws_reserve(c, n)))
     return st;
+  uint32_t epoch;
+  if ((st = next_epoch(c, &epoch)))
+    return st;
   Node* nodes = static_cast<Node*>(bvh->nodes.ptr);
   if (bvh->flags & LBVH_BUILD_SORTED_LEAVES) {
     const uint32_t* perm = static_cast<const uint32_t*>(bvh->leaf_prim.ptr);
     if (kind == kKindTris) {
       Tri* sp = static_cast<Tri*>(bvh->sorted_prims.ptr);
       CK(launch_gather_tris(static_cast<const Tri*>(dprims), perm, n, sp, c->stream), "gather launch");
-      CK(launch_refit_tris(sp, n, c->bufs, nodes, c->stream), "refit launch");
+      CK(launch_refit_tris(sp, n, c->bufs, nodes, epoch, c->stream), "refit launch");
     } else {
       Box* sp = static_cast<Box*>(bvh->sorted_prims.ptr);
       CK(launch_gather_boxes(static_cast<const Box*>(dprims), perm, n, sp, c->stream), "gather launch");
-      CK(launch_refit_boxes(sp, n, c->bufs, nodes, c->stream), "refit launch");
+      CK(launch_refit_boxes(sp, n, c->bufs, nodes, epoch, c->stream), "refit launch");
     }
   } else if (kind == kKindTris) {
-    CK(launch_refit_tris(static_cast<const Tri*>(dprims), n, c->bufs, nodes, c->stream), "refit launch");
+    CK(launch_refit_tris(static_cast<const Tri*>(dprims), n, c->bufs, nodes, epoch, c->stream), "refit launch");
   } else {
-    CK(launch_refit_boxes(static_cast<const Box*>(dprims), n, c->bufs, nodes, c->stream), "refit launch");
+    CK(launch_refit_boxes(static_cast<const Box*>(dprims), n, c->bufs, nodes, epoch, c->stream), "refit launch");
   }
   bvh->prims = dprims;
   bvh->wnodes_valid = false;
@@ -465,7 +470,7 @@ lbvh_ctx_destroy(lbvh_ctx* c)
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   release(c->ws, c->stream);
-  release(c->flags, c->stream);
+  release(c->slots, c->stream);
   release(c->lookback, c->stream);
   release(c->rays, c->stream);
   release(c->hits, c->stream);

@@ -1,12 +1,13 @@
 // LBVH build kernels for sm_103a: centroid bounds, Morton codes + radix
-// histograms, onesweep LSD radix sort, Karras split, bottom-up box fit.
+// histograms, onesweep LSD radix sort, bottom-up tree construction fused with
+// the box fit, and refit.
 //
 // Reference: tay10r/lbvh `lbvh.h`, builder<float>::operator() (lbvh.h:1793-1822).
 // Every kernel reproduces the reference's outputs bit for bit; the comments on
 // each kernel cite the reference code it replaces.
 #include "build.cuh"
 
-#include <cuda/atomic>
+#include <atomic>
 
 namespace lbvh_gb300 {
 
@@ -195,6 +196,7 @@ k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __res
       st->scale[k] = fdiv(1024.0f, fadd(fsub(r.v[k + 3], r.v[k]), 1.0f));
     }
     st->done_counter = 0;
+    st->pending_count = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++)
       st->tile_counter[k] = 0;
@@ -385,19 +387,36 @@ k_onesweep(const uint32_t* __restrict__ kin,
   const uint32_t gofs = block_excl_scan_256(st->hist[pass][tid], s_warp);
   s_tile_start[tid] = block_excl_scan_256(total, s_warp);
 
+  // Decoupled look-back over earlier tiles, kLookbackWindow words per poll:
+  // add aggregates until an inclusive prefix; stop at a word not yet published
+  // and poll again from there.
   uint32_t excl = 0;
   if (tile > 0) {
-    uint32_t p = tile - 1;
+    uint32_t p = tile - 1; // next tile to read
     uint32_t spins = 0;
-    for (;;) {
-      const unsigned long long e = ld_relaxed_u64(lookback + size_t(p) * 256 + tid);
-      const uint32_t lo = uint32_t(e);
-      const uint32_t status = lo >> 30;
-      if (uint32_t(e >> 32) == epoch && status != 0) {
+    bool done = false;
+    while (!done) {
+      unsigned long long e[kLookbackWindow];
+#pragma unroll
+      for (int w = 0; w < kLookbackWindow; w++)
+        e[w] = (uint32_t(w) <= p) ? ld_relaxed_u64(lookback + size_t(p - w) * 256 + tid) : 0ull;
+      uint32_t used = 0;
+#pragma unroll
+      for (int w = 0; w < kLookbackWindow; w++) {
+        if (done || used != uint32_t(w) || uint32_t(w) > p)
+          continue;
+        const uint32_t lo = uint32_t(e[w]);
+        const uint32_t status = lo >> 30;
+        if (uint32_t(e[w] >> 32) != epoch || status == 0)
+          continue; // not yet published: poll again from here
         excl += lo & 0x3fffffffu;
-        if (status == 2 || p == 0)
-          break;
-        --p;
+        used++;
+        done = status == 2 || p - w == 0;
+      }
+      if (done)
+        break;
+      if (used) {
+        p -= used;
         spins = 0;
       } else if (++spins > kSpinLimit) {
         atomicOr(&st->error, kErrLookbackTimeout);
@@ -439,74 +458,302 @@ k_onesweep(const uint32_t* __restrict__ kin,
 }
 
 // ---------------------------------------------------------------------------
-// Karras split, one thread per internal node (divide_node + builder_kernel,
-// lbvh.h:1588-1731). The search is the reference's: direction from
-// delta(i, i+1) - delta(i, i-1), an exponential probe from l_max = 128 in
-// steps of x4, a binary search for the range end, then a binary search for
-// the split with ceil-divided steps. delta is clz of the code xor, or
-// clz(i ^ j) + 32 on equal codes, or -1 out of range.
+// Tree construction fused with the box fit. Replaces the reference's
+// per-node split search (divide_node + builder_kernel, lbvh.h:1588-1731) and
+// its serial fit (builder::fit_boxes, lbvh.h:1826-1867) with one bottom-up
+// pass that produces the identical node array.
+//
+// The reference's tree is the binary radix tree over the sorted codes made
+// distinct by their positions: delta(i, j) = clz(code_i ^ code_j), or
+// clz(i ^ j) + 32 on equal codes, -1 out of range (lbvh.h:1602-1621). Node
+// i's range has i at one end and is split at gamma; its children are gamma
+// (range ending at gamma) and gamma + 1 (range starting there), with the leaf
+// bit when a child range is a single slot (lbvh.h:1718-1729). So a node that
+// is its parent's left child is stored at its range's right end, a right
+// child at its left end, and the root [0, n-1] at 0.
+//
+// Bottom-up: a node [L, R] is its parent's left child exactly when
+// delta(R, R+1) > delta(L-1, L) (the two can never be equal), and the
+// parent's split is then R, else L - 1. One thread starts at every leaf slot;
+// at each node it knows its range, hence its own index, writes its record,
+// and arrives at its parent's slot. The first of the two children to arrive
+// leaves its far range end in the slot and stops; the second reads it, has
+// the parent's range, split and children, fits the parent's box (left box,
+// then union with the right, as the reference does) and carries on upwards.
+//
+// A slot is one 64-bit word {epoch, far end} swapped atomically: a word from
+// an earlier build carries another epoch, so slots are never cleared. A
+// child's node record is published with a fence before the swap, and read
+// after one, only when that child is an internal node; leaf boxes are
+// recomputed from the primitives.
 
 __device__ __forceinline__ int
-split_delta(const uint32_t* __restrict__ codes, int64_t n, int64_t j, uint32_t cj, int64_t k)
+boundary_delta(const uint32_t* __restrict__ codes, uint32_t n, uint32_t k)
 {
-  if (k < 0 || k >= n)
+  if (k >= n - 1) // k = L - 1 wraps for L = 0; k = n - 1 is past the end
     return -1;
-  const uint32_t ck = __ldg(codes + k);
-  if (cj == ck)
-    return __clz(uint32_t(j ^ k)) + 32;
-  return __clz(cj ^ ck);
+  const uint32_t a = __ldg(codes + k), b = __ldg(codes + k + 1);
+  return a == b ? int(__clz(k ^ (k + 1))) + 32 : int(__clz(a ^ b));
 }
 
-__global__ __launch_bounds__(kSplitThreads) void
-k_split(const uint32_t* __restrict__ codes,
-        uint32_t n,
-        uint2* __restrict__ child,
-        uint32_t* __restrict__ leaf_parent,
-        uint32_t* __restrict__ node_parent)
+__device__ __forceinline__ void
+store_node(Node* __restrict__ nodes, uint32_t idx, const Box& b, uint32_t l, uint32_t r)
 {
-  const uint32_t ii = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ii + 1 >= n)
-    return;
-  const int64_t i = ii, nn = n;
-  const uint32_t ci = __ldg(codes + i);
-  const int d = (split_delta(codes, nn, i, ci, i + 1) - split_delta(codes, nn, i, ci, i - 1)) < 0 ? -1 : 1;
-  const int dmin = split_delta(codes, nn, i, ci, i - d);
-  int64_t lmax = 128;
+  float4* dst = reinterpret_cast<float4*>(nodes + idx);
+  __stcg(dst + 0, make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]));
+  __stcg(dst + 1, make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r)));
+}
+
+__device__ __forceinline__ Box
+load_node_box(const Node* __restrict__ nodes, uint32_t idx)
+{
+  const float4 a = __ldcg(reinterpret_cast<const float4*>(nodes + idx));
+  const float2 b = __ldcg(reinterpret_cast<const float2*>(nodes + idx) + 2);
+  return Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
+}
+
+// Two phases.
+//
+// Local phase (k_tree_local), one CTA per kTreeBlock consecutive leaf slots:
+// every node whose range lies inside the CTA's slots finds its parent's
+// arrival slot and its sibling's record in shared memory, and threads walk up
+// with shared-memory atomics and block-scope fences only. Lanes take leaf
+// slots from a CTA queue (one shared atomic per warp refill), so a lane whose
+// walk ended starts the next one instead of idling while its warp finishes.
+// A walk ends at a first arrival, or at a node whose parent's split lies on
+// the CTA's edge (a "CTA root"). After a barrier, a slot holding a single
+// arrival marks a node whose sibling range leaves the CTA. Those nodes and the
+// CTA roots -- the canonical pieces of the CTA's slot range, at most two per
+// tree level -- go to a pending list; the CTA's finished records are written
+// out coalesced.
+//
+// Global phase (k_tree_global), one thread per pending node, launched after
+// the local phase so that CTAs are not held by the long global chains: the
+// same walk over the global epoch-tagged slots. Every record a thread writes
+// is published with a device-scope fence before its next global arrival.
+
+struct PendingNode
+{
+  uint32_t L, R;
+  Box box;
+};
+static_assert(sizeof(PendingNode) == 32, "pending record layout");
+
+constexpr uint32_t kSlotEmpty = 0xffffffffu;    // no arrival yet
+constexpr uint32_t kSlotComplete = 0xfffffffeu; // both children arrived
+
+__device__ __forceinline__ void
+stage_record(Node& rec, const Box& b, uint32_t l, uint32_t r)
+{
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    rec.lo[k] = b.lo[k];
+    rec.hi[k] = b.hi[k];
+  }
+  rec.left = l;
+  rec.right = r;
+}
+
+template<class Leaf>
+__global__ __launch_bounds__(kTreeThreads) void
+k_tree_local(Leaf leaf,
+             uint32_t n,
+             const uint32_t* __restrict__ codes,
+             Node* __restrict__ nodes,
+             PendingNode* __restrict__ pending_out,
+             uint32_t pending_cap,
+             BuildState* __restrict__ st)
+{
+  extern __shared__ __align__(32) unsigned char smem[];
+  int* s_delta = reinterpret_cast<int*>(smem);                               // kTreeBlock + 1
+  uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_delta + kTreeBlock + 8);   // kTreeBlock
+  Node* s_rec = reinterpret_cast<Node*>(s_slot + kTreeBlock);                 // kTreeBlock
+  __shared__ PendingNode s_pend[kTreePendingPerBlock];
+  __shared__ uint32_t s_next, s_npend, s_base;
+
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint32_t b0 = blockIdx.x * kTreeBlock;
+  const uint32_t count = min(kTreeBlock, n - b0);
+
+  // boundaries k = b0 - 1 .. b0 + kTreeBlock - 1 at s_delta[k - (b0 - 1)]
+  for (uint32_t j = tid; j <= kTreeBlock; j += kTreeThreads)
+    s_delta[j] = boundary_delta(codes, n, b0 - 1 + j);
+  for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
+    s_slot[j] = kSlotEmpty;
+    s_rec[j].left = 0; // no record (node 0, the root, is never a child)
+  }
+  if (tid == 0) {
+    s_next = 0;
+    s_npend = 0;
+  }
+  __syncthreads();
+
+  bool active = false, internal = false;
+  uint32_t L = 0, R = 0, lref = 0, rref = 0;
+  Box box{};
+  const uint32_t lt_mask = (1u << lane) - 1u;
   for (;;) {
-    const int64_t k = i + lmax * d;
-    if (k >= nn)
-      break;
-    if (!(split_delta(codes, nn, i, ci, k) > dmin))
-      break;
-    lmax *= 4;
+    // ---- lanes without a walk take the next leaf slots of the CTA ----
+    const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+    if (idle) {
+      uint32_t first = 0;
+      if ((idle & lt_mask) == 0 && !active)
+        first = atomicAdd(&s_next, uint32_t(__popc(idle)));
+      first = __shfl_sync(0xffffffffu, first, __ffs(idle) - 1);
+      if (!active) {
+        const uint32_t j = first + __popc(idle & lt_mask);
+        if (j < count) {
+          L = R = b0 + j;
+          box = leaf(L);
+          internal = false;
+          active = true;
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active))
+      break; // the queue is empty and every walk has ended
+    if (!active)
+      continue;
+
+    // ---- one step of the walk ----
+    const bool is_left = s_delta[R - b0 + 1] > s_delta[L - b0]; // delta(R) vs delta(L - 1)
+    const uint32_t s = is_left ? R : L - 1;
+    if (internal)
+      stage_record(s_rec[(is_left ? R : L) - b0], box, lref, rref);
+    if (s < b0 || s + 1 >= b0 + kTreeBlock) { // split on the CTA's edge
+      const uint32_t k = atomicAdd(&s_npend, 1u);
+      if (k < kTreePendingPerBlock)
+        s_pend[k] = PendingNode{ L, R, box };
+      active = false;
+      continue;
+    }
+    __threadfence_block();
+    const uint32_t old = atomicExch(s_slot + (s - b0), is_left ? L : R);
+    if (old == kSlotEmpty) {
+      active = false; // first arrival: recoverable from the slot if unmatched
+      continue;
+    }
+    s_slot[s - b0] = kSlotComplete;
+    __threadfence_block();
+    const uint32_t LP = is_left ? L : old, RP = is_left ? old : R;
+    const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
+    const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
+    const uint32_t sib = is_left ? cr : cl;
+    Box other;
+    if (sib & kLeafBit) {
+      other = leaf(sib & ~kLeafBit);
+    } else {
+      const Node& o = s_rec[sib - b0];
+      other = Box{ { o.lo[0], o.lo[1], o.lo[2] }, { o.hi[0], o.hi[1], o.hi[2] } };
+    }
+    box = is_left ? join(box, other) : join(other, box);
+    L = LP;
+    R = RP;
+    lref = cl;
+    rref = cr;
+    internal = true;
+    if (L == 0 && R == n - 1) { // the root: the whole tree fits in this CTA
+      stage_record(s_rec[0], box, lref, rref);
+      active = false;
+    }
   }
-  int64_t l = 0;
-  for (int64_t div = 2;; div *= 2) {
-    const int64_t t = lmax / div;
-    if (split_delta(codes, nn, i, ci, i + (l + t) * d) > dmin)
-      l += t;
-    if (t == 1)
-      break;
+  __syncthreads();
+
+  // coalesced write-out of the records finished in this CTA, and the first
+  // arrivals that were never matched
+  for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
+    const Node rec = s_rec[j];
+    if (rec.left != 0 && b0 + j + 1 < n)
+      store_node(nodes, b0 + j, Box{ { rec.lo[0], rec.lo[1], rec.lo[2] }, { rec.hi[0], rec.hi[1], rec.hi[2] } },
+                 rec.left, rec.right);
+    const uint32_t v = s_slot[j];
+    if (v != kSlotEmpty && v != kSlotComplete) {
+      const uint32_t sj = b0 + j;
+      // the waiter was the left child [v, s] (v <= s) or the right [s + 1, v]
+      const uint32_t wl = v <= sj ? v : sj + 1, wr = v <= sj ? sj : v;
+      Box wb;
+      if (wl == wr) {
+        wb = leaf(wl);
+      } else {
+        const Node& o = s_rec[(v <= sj ? wr : wl) - b0];
+        wb = Box{ { o.lo[0], o.lo[1], o.lo[2] }, { o.hi[0], o.hi[1], o.hi[2] } };
+      }
+      const uint32_t k = atomicAdd(&s_npend, 1u);
+      if (k < kTreePendingPerBlock)
+        s_pend[k] = PendingNode{ wl, wr, wb };
+    }
   }
-  const int64_t j = i + l * d;
-  const int dnode = split_delta(codes, nn, i, ci, j);
-  int64_t s = 0;
-  for (int64_t div = 2;; div *= 2) {
-    const int64_t t = (l + (div - 1)) / div;
-    if (split_delta(codes, nn, i, ci, i + (s + t) * d) > dnode)
-      s += t;
-    if (div >= l)
-      break;
+  __syncthreads();
+  const uint32_t np = s_npend;
+  if (tid == 0) {
+    if (np > kTreePendingPerBlock)
+      atomicOr(&st->error, kErrBadTopology); // more canonical pieces than a tree can have
+    s_base = np ? atomicAdd(&st->pending_count, min(np, kTreePendingPerBlock)) : 0;
   }
-  const int64_t gamma = i + s * d + (d < 0 ? d : 0);
-  const int64_t lo = i < j ? i : j;
-  const int64_t hi = j > i ? j : i;
-  const bool lleaf = lo == gamma;
-  const bool rleaf = hi == gamma + 1;
-  child[i] = make_uint2(uint32_t(gamma) | (lleaf ? kLeafBit : 0u),
-                        uint32_t(gamma + 1) | (rleaf ? kLeafBit : 0u));
-  (lleaf ? leaf_parent : node_parent)[gamma] = uint32_t(i);
-  (rleaf ? leaf_parent : node_parent)[gamma + 1] = uint32_t(i);
+  __syncthreads();
+  for (uint32_t k = tid; k < min(np, kTreePendingPerBlock); k += kTreeThreads) {
+    const uint32_t at = s_base + k;
+    if (at < pending_cap)
+      pending_out[at] = s_pend[k];
+    else
+      atomicOr(&st->error, kErrBadTopology);
+  }
+}
+
+template<class Leaf>
+__global__ __launch_bounds__(kFitThreads) void
+k_tree_global(Leaf leaf,
+              uint32_t n,
+              const uint32_t* __restrict__ codes,
+              unsigned long long* __restrict__ slots,
+              Node* __restrict__ nodes,
+              const PendingNode* __restrict__ pending_in,
+              BuildState* __restrict__ st,
+              uint32_t epoch)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= min(__ldg(&st->pending_count), uint32_t(gridDim.x * blockDim.x)))
+    return;
+  const PendingNode pn = pending_in[i];
+  uint32_t L = pn.L, R = pn.R;
+  Box box = pn.box;
+  const unsigned long long tag = (unsigned long long)epoch << 32;
+  bool wrote = false; // records from the local phase are visible at launch
+  for (uint32_t depth = 0;; depth++) {
+    if (depth > kMaxTreeDepth + 2) {
+      atomicOr(&st->error, kErrBadTopology);
+      return;
+    }
+    const bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+    const uint32_t s = is_left ? R : L - 1;
+    if (wrote)
+      __threadfence(); // publish this node's record before the sibling can see the slot
+    const unsigned long long old = atomicExch(slots + s, tag | (is_left ? L : R));
+    if (uint32_t(old >> 32) != epoch)
+      return; // first arrival: the sibling completes the parent
+    const uint32_t far = uint32_t(old);
+    const uint32_t LP = is_left ? L : far, RP = is_left ? far : R;
+    const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
+    const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
+    const uint32_t sib = is_left ? cr : cl;
+    Box other;
+    if (sib & kLeafBit) {
+      other = leaf(sib & ~kLeafBit);
+    } else {
+      __threadfence(); // the sibling's record was published before its swap
+      other = load_node_box(nodes, sib);
+    }
+    box = is_left ? join(box, other) : join(other, box);
+    L = LP;
+    R = RP;
+    if (L == 0 && R == n - 1) {
+      store_node(nodes, 0, box, cl, cr);
+      return;
+    }
+    const bool up_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+    store_node(nodes, up_left ? R : L, box, cl, cr);
+    wrote = true;
+  }
 }
 
 // Parent links from an existing node array (for refit).
@@ -536,28 +783,20 @@ k_links_from_nodes(const Node* __restrict__ nodes,
     node_parent[r] = i;
 }
 
-// ---------------------------------------------------------------------------
-// Bottom-up box fit with per-node arrival flags. Replaces the reference's
-// serial fit (builder::fit_boxes, lbvh.h:1826-1867): node box = left box
-// (leaf converter or child node box), then union_of(box, right box). The
-// union is order-fixed (left first), so the result does not depend on which
-// child arrives last.
-//
-// One thread per leaf slot. Each internal node receives exactly two
-// arrivals per build; the flag word counts them, so the first arrival sees an
-// even value and stops, the second sees an odd one and fits the node. Flags
-// therefore stay even between builds and need no clearing.
-
+// Refit: the box fit alone over a given topology (child and parent links),
+// with the same arrival slots as k_build_tree. Equal to the reference's
+// fit_boxes over the existing nodes.
 template<class Leaf>
 __global__ __launch_bounds__(kFitThreads) void
-k_fit(Leaf leaf,
-      uint32_t n,
-      const uint2* __restrict__ child,
-      const uint32_t* __restrict__ leaf_parent,
-      const uint32_t* __restrict__ node_parent,
-      uint32_t* __restrict__ flags,
-      Node* __restrict__ nodes,
-      BuildState* __restrict__ st)
+k_refit(Leaf leaf,
+        uint32_t n,
+        const uint2* __restrict__ child,
+        const uint32_t* __restrict__ leaf_parent,
+        const uint32_t* __restrict__ node_parent,
+        unsigned long long* __restrict__ slots,
+        Node* __restrict__ nodes,
+        BuildState* __restrict__ st,
+        uint32_t epoch)
 {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n)
@@ -565,14 +804,16 @@ k_fit(Leaf leaf,
   Box box = leaf(p);
   uint32_t self = p | kLeafBit;
   uint32_t q = __ldg(leaf_parent + p);
+  const unsigned long long tag = (unsigned long long)epoch << 32;
   for (uint32_t depth = 0;; depth++) {
     if (q >= n - 1 || depth > 2 * kMaxTreeDepth) {
       atomicOr(&st->error, kErrBadTopology);
       return;
     }
-    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> f(flags[q]);
-    const uint32_t old = f.fetch_add(1u, cuda::memory_order_acq_rel);
-    if ((old & 1u) == 0)
+    if (!(self & kLeafBit))
+      __threadfence(); // publish this node's record before arriving
+    const unsigned long long old = atomicExch(slots + q, tag);
+    if (uint32_t(old >> 32) != epoch)
       return;
     const uint2 lr = __ldg(child + q);
     const uint32_t lx = lr.x & ~kLeafBit, ly = lr.y & ~kLeafBit;
@@ -580,29 +821,16 @@ k_fit(Leaf leaf,
       atomicOr(&st->error, kErrBadTopology);
       return;
     }
-    Box lb, rb;
-    if (lr.x == self)
-      lb = box;
-    else if (lr.x & kLeafBit)
-      lb = leaf(lr.x & ~kLeafBit);
-    else {
-      const float4 a = __ldcg(reinterpret_cast<const float4*>(nodes + lr.x));
-      const float2 b = __ldcg(reinterpret_cast<const float2*>(nodes + lr.x) + 2);
-      lb = Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
+    const uint32_t sib = (lr.x == self) ? lr.y : lr.x;
+    Box other;
+    if (sib & kLeafBit) {
+      other = leaf(sib & ~kLeafBit);
+    } else {
+      __threadfence();
+      other = load_node_box(nodes, sib);
     }
-    if (lr.y == self)
-      rb = box;
-    else if (lr.y & kLeafBit)
-      rb = leaf(lr.y & ~kLeafBit);
-    else {
-      const float4 a = __ldcg(reinterpret_cast<const float4*>(nodes + lr.y));
-      const float2 b = __ldcg(reinterpret_cast<const float2*>(nodes + lr.y) + 2);
-      rb = Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
-    }
-    box = join(lb, rb);
-    float4* dst = reinterpret_cast<float4*>(nodes + q);
-    __stcg(dst + 0, make_float4(box.lo[0], box.lo[1], box.lo[2], box.hi[0]));
-    __stcg(dst + 1, make_float4(box.hi[1], box.hi[2], __uint_as_float(lr.x), __uint_as_float(lr.y)));
+    box = (lr.x == self) ? join(box, other) : join(other, box);
+    store_node(nodes, q, box, lr.x, lr.y);
     if (q == 0)
       return;
     self = q;
@@ -675,11 +903,27 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
 
 template<class Leaf>
 static cudaError_t
-launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s)
+launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
 {
-  k_split<<<ceil_div_u32(n - 1, kSplitThreads), kSplitThreads, 0, s>>>(b.keys_a, n, b.child, b.leaf_parent, b.node_parent);
-  k_fit<Leaf><<<ceil_div_u32(n, kFitThreads), kFitThreads, 0, s>>>(
-    leaf, n, b.child, b.leaf_parent, b.node_parent, b.flags, nodes, b.state);
+  // the shared-memory opt-in is per device; set it once on each
+  static std::atomic<uint64_t> configured{ 0 };
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return e;
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(configured.load(std::memory_order_relaxed) & bit)) {
+    e = cudaFuncSetAttribute(k_tree_local<Leaf>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTreeSmem));
+    if (e != cudaSuccess)
+      return e;
+    configured.fetch_or(bit, std::memory_order_relaxed);
+  }
+  const uint32_t blocks = ceil_div_u32(n, kTreeBlock);
+  const uint32_t cap = blocks * kTreePendingPerBlock;
+  k_tree_local<Leaf><<<blocks, kTreeThreads, kTreeSmem, s>>>(leaf, n, b.keys_a, nodes,
+                                                           reinterpret_cast<PendingNode*>(b.pending), cap, b.state);
+  k_tree_global<Leaf><<<ceil_div_u32(cap, kFitThreads), kFitThreads, 0, s>>>(
+    leaf, n, b.keys_a, b.slots, nodes, reinterpret_cast<const PendingNode*>(b.pending), b.state, epoch);
   return cudaGetLastError();
 }
 
@@ -705,15 +949,15 @@ launch_curve_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, cudaStre
 }
 
 cudaError_t
-launch_fit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s)
+launch_fit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
 {
-  return launch_topology_and_fit(TriLeaf{ tris }, n, b, nodes, s);
+  return launch_topology_and_fit(TriLeaf{ tris }, n, b, nodes, epoch, s);
 }
 
 cudaError_t
-launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s)
+launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
 {
-  return launch_topology_and_fit(BoxLeaf{ boxes }, n, b, nodes, s);
+  return launch_topology_and_fit(BoxLeaf{ boxes }, n, b, nodes, epoch, s);
 }
 
 cudaError_t
@@ -732,24 +976,24 @@ launch_gather_boxes(const Box* boxes, const uint32_t* perm, uint32_t n, Box* out
 
 template<class Leaf>
 static cudaError_t
-launch_refit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s)
+launch_refit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
 {
   k_links_from_nodes<<<ceil_div_u32(n - 1, 256), 256, 0, s>>>(nodes, n - 1, b.child, b.leaf_parent, b.node_parent);
-  k_fit<Leaf><<<ceil_div_u32(n, kFitThreads), kFitThreads, 0, s>>>(
-    leaf, n, b.child, b.leaf_parent, b.node_parent, b.flags, nodes, b.state);
+  k_refit<Leaf><<<ceil_div_u32(n, kFitThreads), kFitThreads, 0, s>>>(
+    leaf, n, b.child, b.leaf_parent, b.node_parent, b.slots, nodes, b.state, epoch);
   return cudaGetLastError();
 }
 
 cudaError_t
-launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s)
+launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
 {
-  return launch_refit(TriLeaf{ tris }, n, b, nodes, s);
+  return launch_refit(TriLeaf{ tris }, n, b, nodes, epoch, s);
 }
 
 cudaError_t
-launch_refit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s)
+launch_refit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
 {
-  return launch_refit(BoxLeaf{ boxes }, n, b, nodes, s);
+  return launch_refit(BoxLeaf{ boxes }, n, b, nodes, epoch, s);
 }
 
 } // namespace lbvh_gb300

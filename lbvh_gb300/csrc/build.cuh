@@ -13,9 +13,18 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems; // 4096 keys per tile
-constexpr int kSplitThreads = 256;
 constexpr int kFitThreads = 256;
+constexpr uint32_t kTreeBlock = 1024; // leaf slots per CTA of the tree build
+// Pending-list capacity per CTA: the canonical pieces of a slot range number
+// at most two per tree level, and the tree has at most 63 levels.
+constexpr uint32_t kTreePendingPerBlock = 128;
+constexpr uint32_t kTreeThreads = 256; // threads per CTA of the tree build (4 slots each)
+// dynamic shared memory of the tree build: deltas, slots, node records (each
+// array starts on a 32-byte boundary)
+constexpr size_t kTreeSmem = (kTreeBlock + 8) * 4 + kTreeBlock * 4 + kTreeBlock * 32;
+static_assert(((kTreeBlock + 8) * 4) % 32 == 0 && (kTreeBlock * 4) % 32 == 0, "smem alignment");
 constexpr uint32_t kSpinLimit = 1u << 22;   // look-back polls before giving up
+constexpr int kLookbackWindow = 8;          // look-back words read per poll
 constexpr uint32_t kMaxTreeDepth = 64;      // 30-bit codes + 32-bit index tie-break
 constexpr uint32_t kMaxPrims = (1u << 30) - 1; // look-back counts are 30-bit
 
@@ -47,10 +56,11 @@ struct BuildBuffers
   uint32_t* vals_a;               // sort permutation (pairs mode)
   uint32_t* vals_b;
   unsigned long long* lookback;   // tiles x 256 look-back words
-  uint2* child;                   // n-1 {left, right}
-  uint32_t* leaf_parent;          // n
-  uint32_t* node_parent;          // n-1
-  uint32_t* flags;                // n-1 arrival counters (persistent, even)
+  uint2* child;                   // refit: n-1 {left, right}
+  uint32_t* leaf_parent;          // refit: n
+  uint32_t* node_parent;          // refit: n-1
+  unsigned long long* slots;      // n-1 epoch-tagged arrival slots (persistent)
+  void* pending;                  // tree build: 32 B x kTreePendingPerBlock per CTA
   uint32_t bounds_blocks;
   uint32_t morton_blocks;
 };
@@ -59,11 +69,18 @@ cudaError_t launch_make_triangles(const float* verts, uint32_t n, Tri* out, cuda
 cudaError_t launch_curve_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, cudaStream_t s);
 cudaError_t launch_curve_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, cudaStream_t s);
 cudaError_t launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s);
-cudaError_t launch_fit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
-cudaError_t launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
+// Tree construction + box fit from the sorted codes in keys_a; `epoch` tags
+// this build's arrival slots and must differ from every earlier one on the
+// same slots.
+cudaError_t launch_fit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
+                            cudaStream_t s);
+cudaError_t launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
+                             cudaStream_t s);
 cudaError_t launch_gather_tris(const Tri* tris, const uint32_t* perm, uint32_t n, Tri* out, cudaStream_t s);
 cudaError_t launch_gather_boxes(const Box* boxes, const uint32_t* perm, uint32_t n, Box* out, cudaStream_t s);
-cudaError_t launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
-cudaError_t launch_refit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, cudaStream_t s);
+cudaError_t launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
+                              cudaStream_t s);
+cudaError_t launch_refit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
+                               cudaStream_t s);
 
 } // namespace lbvh_gb300

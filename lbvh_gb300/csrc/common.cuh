@@ -15,10 +15,9 @@ namespace lbvh_gb300 {
 constexpr uint32_t kLeafBit = 0x80000000u; // highest_bit<u32>(), lbvh.h:170-175
 constexpr uint32_t kMiss = 0xffffffffu;    // intersection_container miss, lbvh.h:366
 
-// Sticky device error bits (BuildState::error, TraceState error word).
+// Sticky device error bits (BuildState::error).
 constexpr uint32_t kErrLookbackTimeout = 1u << 0;
 constexpr uint32_t kErrBadTopology = 1u << 1;
-constexpr uint32_t kErrFitTimeout = 1u << 2;
 
 // reference triangle<float> (lbvh.h:1959-1983): {p0, e0, e1, normal},
 // 48 bytes = three 16-byte vectors:
@@ -48,7 +47,8 @@ struct __align__(16) Hit
   float t, u, v;
 };
 
-// Device-side state of one build (lives in the context workspace).
+// Device-side state of a build, one per context (persistent, so the sticky
+// error word survives workspace growth).
 struct BuildState
 {
   float lo[3], hi[3];          // centroid bounds
@@ -57,8 +57,9 @@ struct BuildState
   uint32_t hist[4][256];       // radix digit histograms of the Morton codes
   uint32_t tile_counter[4];    // onesweep tile id dispensers, one per pass
   uint32_t done_counter;       // last-block detection in the bounds kernel
+  uint32_t pending_count;      // tree build: nodes left for the global phase
   uint32_t error;              // sticky kErr* bits
-  uint32_t pad1[2];
+  uint32_t pad1;
 };
 
 // ---- exact scalar ops --------------------------------------------------

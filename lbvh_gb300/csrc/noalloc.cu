@@ -10,11 +10,11 @@
 // array; everything else the build needs lives in one file-scope device array
 // below.
 //
-// The scratch array is fixed at kNoAllocMaxPrims primitives (about 1.8 MB).
+// The scratch array is fixed at kNoAllocMaxPrims primitives (about 1.4 MB).
 // Every GPU that loads this library reserves it until the process exits.
 // All calls on a device share it and it keeps the last call's contents, so
-// each call clears the parts that must start at zero (the build counters, the
-// error word and the arrival flags). Calls whose work overlaps on the GPU --
+// each call clears the parts that must start at zero (the build counters and
+// the error word). Calls whose work overlaps on the GPU --
 // two streams, or two host threads -- race on the array and corrupt each
 // other's results: serialize them per device.
 //
@@ -49,11 +49,10 @@ constexpr size_t kOffPartials = kOffState + round_up(sizeof(BuildState));
 constexpr size_t kOffKeysA = kOffPartials + round_up(kBoundsBlocksMax * 48);
 constexpr size_t kOffKeysB = kOffKeysA + round_up(4 * kNoAllocMaxPrims);
 constexpr size_t kOffLookback = kOffKeysB + round_up(4 * kNoAllocMaxPrims);
-constexpr size_t kOffChild = kOffLookback + round_up(kTiles * 256 * 8);
-constexpr size_t kOffLeafParent = kOffChild + round_up(8 * kNoAllocMaxPrims);
-constexpr size_t kOffNodeParent = kOffLeafParent + round_up(4 * kNoAllocMaxPrims);
-constexpr size_t kOffFlags = kOffNodeParent + round_up(4 * kNoAllocMaxPrims);
-constexpr size_t kScratchBytes = kOffFlags + round_up(4 * kNoAllocMaxPrims);
+constexpr size_t kOffSlots = kOffLookback + round_up(kTiles * 256 * 8);
+constexpr size_t kTreeBlocks = (kNoAllocMaxPrims + kTreeBlock - 1) / kTreeBlock;
+constexpr size_t kOffPending = kOffSlots + round_up(8 * kNoAllocMaxPrims);
+constexpr size_t kScratchBytes = kOffPending + round_up(32 * kTreePendingPerBlock * kTreeBlocks);
 
 // The scratch memory of every allocation-free build on this device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -66,7 +65,7 @@ struct DeviceSlot
   cudaError_t setup_error = cudaSuccess;
   unsigned char* scratch = nullptr; // device address of g_noalloc_scratch
   int num_sms = 1;
-  uint32_t epoch = 0;               // look-back epoch of the last call
+  uint32_t epoch = 0;               // epoch of the last call (look-back words, slots)
 };
 
 DeviceSlot g_slots[kMaxDevices];
@@ -139,10 +138,11 @@ lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint3
   b.vals_a = nullptr; // parity build: key-only sort
   b.vals_b = nullptr;
   b.lookback = reinterpret_cast<unsigned long long*>(base + kOffLookback);
-  b.child = reinterpret_cast<uint2*>(base + kOffChild);
-  b.leaf_parent = reinterpret_cast<uint32_t*>(base + kOffLeafParent);
-  b.node_parent = reinterpret_cast<uint32_t*>(base + kOffNodeParent);
-  b.flags = reinterpret_cast<uint32_t*>(base + kOffFlags);
+  b.child = nullptr; // refit links: not used by a build
+  b.leaf_parent = nullptr;
+  b.node_parent = nullptr;
+  b.slots = reinterpret_cast<unsigned long long*>(base + kOffSlots);
+  b.pending = base + kOffPending;
   const uint32_t want = (nn + kBoundsThreads * 8 - 1) / (kBoundsThreads * 8);
   const uint32_t cap = uint32_t(slot.num_sms) * 4;
   b.bounds_blocks = want < 1 ? 1 : (want > cap ? cap : want);
@@ -150,19 +150,21 @@ lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint3
   const uint32_t mcap = uint32_t(slot.num_sms) * 8;
   b.morton_blocks = mwant < 1 ? 1 : (mwant > mcap ? mcap : mwant);
 
-  // What must start at zero: the bounds/sort counters and the error word,
-  // and the arrival flags (an earlier call that failed can leave them odd).
+  // What must start at zero: the bounds/sort counters and the error word.
+  // The look-back words and the tree's arrival slots carry the epoch of the
+  // call that wrote them and are cleared only when the epoch counter starts
+  // (or restarts after wrapping).
   cudaError_t e = cudaMemsetAsync(b.state, 0, sizeof(BuildState), s);
-  if (e == cudaSuccess)
-    e = cudaMemsetAsync(b.flags, 0, 4 * (n - 1), s);
   if (e == cudaSuccess && epoch == 4)
     e = cudaMemsetAsync(b.lookback, 0, kTiles * 256 * 8, s);
+  if (e == cudaSuccess && epoch == 4)
+    e = cudaMemsetAsync(b.slots, 0, 8 * kNoAllocMaxPrims, s);
   if (e == cudaSuccess)
     e = launch_curve_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, s);
   if (e == cudaSuccess)
     e = launch_sort(nn, false, epoch, b, s);
   if (e == cudaSuccess)
-    e = launch_fit_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, static_cast<Node*>(d_nodes), s);
+    e = launch_fit_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, static_cast<Node*>(d_nodes), epoch, s);
   if (e == cudaSuccess && d_status)
     e = cudaMemcpyAsync(d_status, &b.state->error, 4, cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) {
