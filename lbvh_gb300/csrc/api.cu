@@ -183,6 +183,7 @@ ws_reserve(lbvh_ctx* c, size_t n)
   const size_t o_lp = take(4 * n);
   const size_t o_np = take(4 * n);
   const size_t o_pend = take(32 * size_t(kTreePendingPerBlock) * ((n + kTreeBlock - 1) / kTreeBlock));
+  const size_t o_boxes = take(24 * n);
   CK(reserve(c->ws, off, c->stream), "workspace allocation");
   // The look-back buffer only ever holds look-back words: fresh words read as
   // "not published" (epoch 0 is never used), so it is cleared only on growth.
@@ -209,6 +210,7 @@ ws_reserve(lbvh_ctx* c, size_t n)
   b.leaf_parent = reinterpret_cast<uint32_t*>(base + o_lp);
   b.node_parent = reinterpret_cast<uint32_t*>(base + o_np);
   b.pending = base + o_pend;
+  b.boxes = reinterpret_cast<Box*>(base + o_boxes);
   b.slots = static_cast<unsigned long long*>(c->slots.ptr);
   c->ws_prims = n;
   return LBVH_OK;
@@ -328,7 +330,7 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
     }
   } else {
     if (kind == kKindTris)
-      CK(launch_fit_tris(static_cast<const Tri*>(dprims), nn, b, nodes, epoch, c->stream), "fit launch");
+      CK(launch_fit_staged(nn, b, nodes, epoch, c->stream), "fit launch");
     else
       CK(launch_fit_boxes(static_cast<const Box*>(dprims), nn, b, nodes, epoch, c->stream), "fit launch");
   }

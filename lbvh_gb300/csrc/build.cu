@@ -134,7 +134,7 @@ block_reduce_arg(ArgBox a, ArgBox* s_part)
 
 template<class Leaf>
 __global__ __launch_bounds__(kBoundsThreads) void
-k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __restrict__ st)
+k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __restrict__ st, Box* __restrict__ box_out)
 {
   __shared__ ArgBox s_part[kBoundsThreads / 32];
   __shared__ bool s_last;
@@ -144,6 +144,12 @@ k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __res
   ArgBox a = empty_arg();
   for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     const Box bx = leaf(i);
+    if (box_out) { // stage the leaf box: later passes read 24 bytes, not 48
+      float2* o = reinterpret_cast<float2*>(box_out + i);
+      o[0] = make_float2(bx.lo[0], bx.lo[1]);
+      o[1] = make_float2(bx.lo[2], bx.hi[0]);
+      o[2] = make_float2(bx.hi[1], bx.hi[2]);
+    }
     // center_of, lbvh.h:1160-1167: (min + max) * 0.5
     const float c[3] = { fmul(fadd(bx.lo[0], bx.hi[0]), 0.5f),
                          fmul(fadd(bx.lo[1], bx.hi[1]), 0.5f),
@@ -869,10 +875,14 @@ k_gather_boxes(const Box* __restrict__ boxes,
 
 template<class Leaf>
 static cudaError_t
-launch_curve(const Leaf& leaf, uint32_t n, const BuildBuffers& b, cudaStream_t s)
+launch_curve(const Leaf& leaf, uint32_t n, const BuildBuffers& b, cudaStream_t s, Box* stage)
 {
-  k_bounds<Leaf><<<b.bounds_blocks, kBoundsThreads, 0, s>>>(leaf, n, reinterpret_cast<ArgBox*>(b.partials), b.state);
-  k_morton<Leaf><<<b.morton_blocks, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state);
+  k_bounds<Leaf><<<b.bounds_blocks, kBoundsThreads, 0, s>>>(leaf, n, reinterpret_cast<ArgBox*>(b.partials), b.state,
+                                                            stage);
+  if (stage)
+    k_morton<BoxLeaf><<<b.morton_blocks, kMortonThreads, 0, s>>>(BoxLeaf{ stage }, n, b.keys_a, b.state);
+  else
+    k_morton<Leaf><<<b.morton_blocks, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state);
   return cudaGetLastError();
 }
 
@@ -939,13 +949,19 @@ launch_make_triangles(const float* verts, uint32_t n, Tri* out, cudaStream_t s)
 cudaError_t
 launch_curve_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, cudaStream_t s)
 {
-  return launch_curve(TriLeaf{ tris }, n, b, s);
+  return launch_curve(TriLeaf{ tris }, n, b, s, b.boxes);
 }
 
 cudaError_t
 launch_curve_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, cudaStream_t s)
 {
-  return launch_curve(BoxLeaf{ boxes }, n, b, s);
+  return launch_curve(BoxLeaf{ boxes }, n, b, s, nullptr);
+}
+
+cudaError_t
+launch_fit_staged(uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s)
+{
+  return launch_topology_and_fit(BoxLeaf{ b.boxes }, n, b, nodes, epoch, s);
 }
 
 cudaError_t

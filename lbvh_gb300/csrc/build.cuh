@@ -61,11 +61,15 @@ struct BuildBuffers
   uint32_t* node_parent;          // refit: n-1
   unsigned long long* slots;      // n-1 epoch-tagged arrival slots (persistent)
   void* pending;                  // tree build: 32 B x kTreePendingPerBlock per CTA
+  Box* boxes;                     // optional: leaf boxes staged by the bounds pass (n)
   uint32_t bounds_blocks;
   uint32_t morton_blocks;
 };
 
 cudaError_t launch_make_triangles(const float* verts, uint32_t n, Tri* out, cudaStream_t s);
+// Bounds + Morton codes; with b.boxes set, also stages the leaf boxes there
+// (input order) so the Morton pass and launch_fit_staged read 24 bytes per
+// leaf instead of the 48-byte triangle.
 cudaError_t launch_curve_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, cudaStream_t s);
 cudaError_t launch_curve_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, cudaStream_t s);
 cudaError_t launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s);
@@ -76,6 +80,8 @@ cudaError_t launch_fit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, 
                             cudaStream_t s);
 cudaError_t launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
                              cudaStream_t s);
+// Tree + fit over the leaf boxes staged by launch_curve_tris (input order).
+cudaError_t launch_fit_staged(uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s);
 cudaError_t launch_gather_tris(const Tri* tris, const uint32_t* perm, uint32_t n, Tri* out, cudaStream_t s);
 cudaError_t launch_gather_boxes(const Box* boxes, const uint32_t* perm, uint32_t n, Box* out, cudaStream_t s);
 cudaError_t launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
