@@ -151,6 +151,17 @@ LBVH_API int lbvh_build_boxes(lbvh_ctx* ctx, const float* boxes, size_t n, uint3
 LBVH_API int lbvh_refit_triangles(lbvh_ctx* ctx, lbvh_bvh* bvh, const float* tris);
 LBVH_API int lbvh_refit_boxes(lbvh_ctx* ctx, lbvh_bvh* bvh, const float* boxes);
 
+/* Makes `bvh` from an existing node array (n_nodes x 32 bytes, host or
+ * device, e.g. a reference lbvh::bvh<float>, lbvh.h:259-299) and its
+ * n_nodes + 1 triangles, for lbvh_trace_triangles -- the reference traverser's
+ * constructor traverser(const bvh<float>&, const triangle<float>*)
+ * (lbvh.h:520-524). The nodes are copied; the check_bvh invariants
+ * (lbvh_test.cpp:369-446) are verified on the device and a violation returns
+ * LBVH_ERR_BAD_TOPOLOGY. Synchronizes. Same borrowing rule for device
+ * triangles as lbvh_build_triangles. */
+LBVH_API int lbvh_bvh_import_triangles(lbvh_ctx* ctx, const void* nodes, size_t n_nodes, const float* tris,
+                                       lbvh_bvh* bvh);
+
 /* Replaces bvh<float>::size() (lbvh.h:274): n_prims, n_nodes = n_prims - 1. */
 LBVH_API int lbvh_bvh_info(const lbvh_bvh* bvh, size_t* n_prims, size_t* n_nodes, uint32_t* flags);
 /* Replaces bvh<float>::begin()/operator[] (lbvh.h:270-292): copies the

@@ -51,6 +51,7 @@ SIGNATURES = {
     "lbvh_build_boxes": (_I, [_P, _P, _S, _U32, _P]),
     "lbvh_refit_triangles": (_I, [_P, _P, _P]),
     "lbvh_refit_boxes": (_I, [_P, _P, _P]),
+    "lbvh_bvh_import_triangles": (_I, [_P, _P, _S, _P, _P]),
     "lbvh_bvh_info": (_I, [_P, ctypes.POINTER(_S), ctypes.POINTER(_S), ctypes.POINTER(_U32)]),
     "lbvh_bvh_nodes": (_I, [_P, _P, _P]),
     "lbvh_bvh_device_nodes": (_P, [_P]),

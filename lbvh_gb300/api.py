@@ -222,6 +222,26 @@ class BVH:
                                                  _addr(perm), _addr(bounds)))
         return codes, sc, perm, bounds
 
+    @classmethod
+    def from_nodes(cls, nodes, triangles, ctx: Context | None = None) -> "BVH":
+        """A BVH over an existing node array (NODE_DTYPE records, e.g. one
+        made by the reference's builder) and its n_nodes + 1 triangles, for
+        tracing. The array is checked on the device (LbvhError on a node
+        array that is not a tree over its leaves)."""
+        bvh = cls(ctx)
+        if isinstance(nodes, np.ndarray):
+            nodes = np.ascontiguousarray(nodes)
+            n_nodes = nodes.nbytes // 32
+        else:
+            n_nodes = nodes.numel() * nodes.element_size() // 32
+        if _rows(triangles, 12, "triangles") != n_nodes + 1:
+            raise ValueError("need n_nodes + 1 triangles")
+        bvh.ctx.check(_lib.lib().lbvh_bvh_import_triangles(bvh.ctx.handle, _addr(nodes), n_nodes,
+                                                          _addr(triangles), bvh.handle))
+        bvh.kind = TRIANGLES
+        bvh._keep = triangles if _is_cuda(triangles) else None
+        return bvh
+
     def refit(self, primitives):
         """Recompute all node boxes over moved primitives (same count and
         order as the build input), keeping the topology."""

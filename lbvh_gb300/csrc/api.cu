@@ -628,6 +628,44 @@ lbvh_refit_boxes(lbvh_ctx* c, lbvh_bvh* bvh, const float* boxes)
 }
 
 int
+lbvh_bvh_import_triangles(lbvh_ctx* c, const void* nodes, size_t n_nodes, const float* tris, lbvh_bvh* bvh)
+{
+  if (!c || !nodes || !tris || !bvh)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (n_nodes < 1 || n_nodes + 1 > kMaxPrims)
+    return fail(c, LBVH_ERR_INVALID_ARG, "node count %zu outside [1, %u]", n_nodes, kMaxPrims - 1);
+  int st = set_device(c);
+  if (st)
+    return st;
+  const size_t n = n_nodes + 1;
+  CK(reserve(bvh->nodes, sizeof(Node) * n_nodes, c->stream), "node allocation");
+  CK(cudaMemcpyAsync(bvh->nodes.ptr, nodes, sizeof(Node) * n_nodes, cudaMemcpyDefault, c->stream), "node upload");
+  const void* dprims = tris;
+  if (!on_device(tris)) {
+    CK(reserve(bvh->prims_owned, sizeof(Tri) * n, c->stream), "primitive allocation");
+    CK(cudaMemcpyAsync(bvh->prims_owned.ptr, tris, sizeof(Tri) * n, cudaMemcpyHostToDevice, c->stream),
+       "primitive upload");
+    dprims = bvh->prims_owned.ptr;
+  } else if (reinterpret_cast<uintptr_t>(tris) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device triangles must be 16-byte aligned");
+  }
+  if ((st = ws_reserve(c, n)))
+    return st;
+  CK(launch_validate(static_cast<const Node*>(bvh->nodes.ptr), uint32_t(n_nodes), c->bufs, c->stream),
+     "validation launch");
+  bvh->n = 0; // unusable until validated
+  if ((st = check_device(c)))
+    return st;
+  bvh->n = uint32_t(n);
+  bvh->flags = 0;
+  bvh->kind = kKindTris;
+  bvh->prims = dprims;
+  bvh->device = c->device;
+  bvh->wnodes_valid = false;
+  return LBVH_OK;
+}
+
+int
 lbvh_bvh_info(const lbvh_bvh* b, size_t* n_prims, size_t* n_nodes, uint32_t* flags)
 {
   if (!b)

@@ -789,6 +789,51 @@ k_links_from_nodes(const Node* __restrict__ nodes,
     node_parent[r] = i;
 }
 
+// Validation of a node array from outside this library (the check_bvh
+// invariants of lbvh_test.cpp:369-446): every child index in range, the root
+// unreferenced, every other internal node and every leaf referenced exactly
+// once. Such an array is a tree below the root, so a traversal from the root
+// visits each node at most once.
+__global__ void
+k_count_refs(const Node* __restrict__ nodes,
+             uint32_t n_nodes,
+             uint32_t* __restrict__ node_refs,
+             uint32_t* __restrict__ leaf_refs,
+             BuildState* __restrict__ st)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_nodes)
+    return;
+  const uint4 lr = *reinterpret_cast<const uint4*>(&nodes[i].hi[1]);
+  const uint32_t c[2] = { lr.z, lr.w };
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const uint32_t x = c[k] & ~kLeafBit;
+    if (c[k] & kLeafBit) {
+      if (x > n_nodes)
+        atomicOr(&st->error, kErrBadTopology);
+      else
+        atomicAdd(leaf_refs + x, 1u);
+    } else {
+      if (x >= n_nodes)
+        atomicOr(&st->error, kErrBadTopology);
+      else
+        atomicAdd(node_refs + x, 1u);
+    }
+  }
+}
+
+__global__ void
+k_check_refs(uint32_t n_nodes, const uint32_t* __restrict__ node_refs, const uint32_t* __restrict__ leaf_refs,
+             BuildState* __restrict__ st)
+{
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_nodes && node_refs[i] != (i == 0 ? 0u : 1u))
+    atomicOr(&st->error, kErrBadTopology);
+  if (i <= n_nodes && leaf_refs[i] != 1u)
+    atomicOr(&st->error, kErrBadTopology);
+}
+
 // Refit: the box fit alone over a given topology (child and parent links),
 // with the same arrival slots as k_build_tree. Equal to the reference's
 // fit_boxes over the existing nodes.
@@ -997,6 +1042,19 @@ launch_refit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Node* nodes, u
   k_links_from_nodes<<<ceil_div_u32(n - 1, 256), 256, 0, s>>>(nodes, n - 1, b.child, b.leaf_parent, b.node_parent);
   k_refit<Leaf><<<ceil_div_u32(n, kFitThreads), kFitThreads, 0, s>>>(
     leaf, n, b.child, b.leaf_parent, b.node_parent, b.slots, nodes, b.state, epoch);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_validate(const Node* nodes, uint32_t n_nodes, const BuildBuffers& b, cudaStream_t s)
+{
+  cudaError_t e = cudaMemsetAsync(b.node_parent, 0, 4 * size_t(n_nodes), s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b.leaf_parent, 0, 4 * (size_t(n_nodes) + 1), s);
+  if (e != cudaSuccess)
+    return e;
+  k_count_refs<<<ceil_div_u32(n_nodes, 256), 256, 0, s>>>(nodes, n_nodes, b.node_parent, b.leaf_parent, b.state);
+  k_check_refs<<<ceil_div_u32(n_nodes + 1, 256), 256, 0, s>>>(n_nodes, b.node_parent, b.leaf_parent, b.state);
   return cudaGetLastError();
 }
 

@@ -84,6 +84,9 @@ cudaError_t launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b
 cudaError_t launch_fit_staged(uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch, cudaStream_t s);
 cudaError_t launch_gather_tris(const Tri* tris, const uint32_t* perm, uint32_t n, Tri* out, cudaStream_t s);
 cudaError_t launch_gather_boxes(const Box* boxes, const uint32_t* perm, uint32_t n, Box* out, cudaStream_t s);
+// Checks an outside node array (n_nodes internal nodes, n_nodes + 1 leaves)
+// with leaf_parent / node_parent as counters; sets kErrBadTopology on failure.
+cudaError_t launch_validate(const Node* nodes, uint32_t n_nodes, const BuildBuffers& b, cudaStream_t s);
 cudaError_t launch_refit_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,
                               cudaStream_t s);
 cudaError_t launch_refit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* nodes, uint32_t epoch,

@@ -100,3 +100,28 @@ def test_user_box_bvh_has_no_triangle_traverser(ctx):
     b = lb.Builder(ctx)(np.zeros((4, 6), np.float32), converter=lb.BOXES)
     with pytest.raises(ValueError):
         lb.Traverser(b)
+
+
+@pytest.mark.parametrize("name", ["soup968", "teapot", "dups4000"])
+def test_trace_imported_reference_nodes(ctx, name):
+    # a node array made by the reference itself, traced on the GPU
+    g = load_golden(name)
+    bvh = lb.BVH.from_nodes(g["nodes"], g["tris"], ctx)
+    assert_hits_equal(lb.Traverser(bvh)(g["rays"]), g["hits"])
+    bvh = lb.BVH.from_nodes(dev(g["nodes"].view(np.uint8)), dev(g["tris"]), ctx)
+    assert_hits_equal(lb.Traverser(bvh)(g["rays"]), g["hits"])
+
+
+def test_import_rejects_malformed_trees(ctx):
+    g = load_golden("soup968")
+    bad = g["nodes"].copy()
+    bad["left"][3] = bad["left"][4]  # a node referenced twice, another lost
+    with pytest.raises(lb.LbvhError):
+        lb.BVH.from_nodes(bad, g["tris"], ctx)
+    bad = g["nodes"].copy()
+    bad["right"][7] = 5000  # an internal index out of range
+    with pytest.raises(lb.LbvhError):
+        lb.BVH.from_nodes(bad, g["tris"], ctx)
+    # the context stays usable
+    ok = lb.BVH.from_nodes(g["nodes"], g["tris"], ctx)
+    assert_hits_equal(lb.Traverser(ok)(g["rays"]), g["hits"])
