@@ -118,6 +118,7 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
  * they tune the GPU kernels, not the results. */
 #define LBVH_PARAM_TRACE_BLOCKS_PER_SM 1 /* persistent traversal grid, 1..32 */
 #define LBVH_PARAM_TRACE_REFILL 2        /* idle lanes before a warp refills, 1..32 */
+#define LBVH_PARAM_BATCH_THREADS 3       /* CTA size of the batched build, 256..1024 */
 LBVH_API int lbvh_ctx_set_param(lbvh_ctx* ctx, int param, int value);
 
 /* Replaces the reference triangle constructor triangle<float>(a, b, c)
@@ -184,6 +185,30 @@ LBVH_API int lbvh_trace_triangles(lbvh_ctx* ctx, const lbvh_bvh* bvh, const floa
 /* Same, also writing per-ray counts of box tests and triangle tests. */
 LBVH_API int lbvh_trace_triangles_counts(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m,
                                 void* hits, uint32_t* n_box, uint32_t* n_tri);
+
+/* ---- batched meshes --------------------------------------------------
+ * Many independent meshes built and traced together. No single reference
+ * counterpart: the batch equals running lbvh::builder<float> (lbvh.h:1793-1822)
+ * and lbvh::traverser (lbvh.h:1869-1942) once per mesh. Mesh k's triangles are
+ * [offsets[k], offsets[k + 1]) of one concatenated array (each mesh >= 2);
+ * its node block starts at node offsets[k] - k, holds offsets[k + 1] -
+ * offsets[k] - 1 nodes with mesh-local indices, and is bit-identical to the
+ * reference's node array for that mesh alone. */
+typedef struct lbvh_batch lbvh_batch;
+LBVH_API int lbvh_batch_create(lbvh_ctx* ctx, lbvh_batch** out);
+LBVH_API int lbvh_batch_destroy(lbvh_ctx* ctx, lbvh_batch* batch);
+/* Builds every mesh in one persistent launch (one CTA per mesh at a time).
+ * offsets: n_meshes + 1 uint32 (host or device); a bad device-side offsets
+ * array is reported as LBVH_ERR_BAD_TOPOLOGY by the next synchronizing call. */
+LBVH_API int lbvh_batch_build_triangles(lbvh_ctx* ctx, const float* tris, size_t total, const uint32_t* offsets,
+                                        size_t n_meshes, lbvh_batch* batch);
+LBVH_API int lbvh_batch_info(const lbvh_batch* batch, size_t* n_meshes, size_t* total_prims, size_t* total_nodes);
+/* Copies all node blocks (total_prims - n_meshes nodes of 32 bytes). */
+LBVH_API int lbvh_batch_nodes(lbvh_ctx* ctx, const lbvh_batch* batch, void* dst);
+/* Traces rays [ray_offsets[k], ray_offsets[k + 1]) against mesh k (m rays in
+ * all, n_meshes + 1 offsets); hit primitive ids are mesh-local. */
+LBVH_API int lbvh_batch_trace_triangles(lbvh_ctx* ctx, const lbvh_batch* batch, const float* rays,
+                                        const uint32_t* ray_offsets, size_t m, void* hits);
 
 /* Largest primitive count lbvh_build_triangles_noalloc accepts. */
 #define LBVH_NOALLOC_MAX_PRIMS 65536u

@@ -6,6 +6,7 @@ include/lbvh_gb300.h); this package is its Python host interface.
 """
 from .api import (  # noqa: F401
     BOXES,
+    Batch,
     BVH,
     HIT_DTYPE,
     LEAF_BIT,

@@ -23,6 +23,7 @@ LBVH_ERR_BAD_TOPOLOGY = 5
 NOALLOC_MAX_PRIMS = 65536
 PARAM_TRACE_BLOCKS_PER_SM = 1
 PARAM_TRACE_REFILL = 2
+PARAM_BATCH_THREADS = 3
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000
@@ -59,6 +60,12 @@ SIGNATURES = {
     "lbvh_trace_triangles": (_I, [_P, _P, _P, _S, _P]),
     "lbvh_trace_triangles_counts": (_I, [_P, _P, _P, _S, _P, _P, _P]),
     "lbvh_build_triangles_noalloc": (_I, [_P, _S, _P, _P, _P]),
+    "lbvh_batch_create": (_I, [_P, _PP]),
+    "lbvh_batch_destroy": (_I, [_P, _P]),
+    "lbvh_batch_build_triangles": (_I, [_P, _P, _S, _P, _S, _P]),
+    "lbvh_batch_info": (_I, [_P, ctypes.POINTER(_S), ctypes.POINTER(_S), ctypes.POINTER(_S)]),
+    "lbvh_batch_nodes": (_I, [_P, _P, _P]),
+    "lbvh_batch_trace_triangles": (_I, [_P, _P, _P, _P, _S, _P]),
 }
 
 

@@ -355,3 +355,85 @@ def hits_view(t) -> np.ndarray:
     """HIT_DTYPE view of a [m, 4] float32 hits tensor copied to the host."""
     a = t.detach().cpu().numpy() if _is_tensor(t) else np.asarray(t)
     return np.ascontiguousarray(a).view(HIT_DTYPE).reshape(-1)
+
+
+def _u32(x, name):
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.uint32:
+            raise ValueError(f"{name} must be uint32")
+        return x
+    if _is_tensor(x):
+        if x.dtype not in (torch.int32, getattr(torch, "uint32", torch.int32)):
+            raise ValueError(f"{name} must be a 32-bit integer tensor")
+        return x
+    return np.ascontiguousarray(x, dtype=np.uint32)
+
+
+class Batch:
+    """Many independent meshes built and traced together (one persistent
+    launch each). Mesh k is triangles [offsets[k], offsets[k + 1]) of one
+    concatenated [total, 12] array; the result per mesh equals the reference
+    builder / traverser run on that mesh alone (mesh-local node and primitive
+    indices)."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        h = ctypes.c_void_p()
+        self.ctx.check(_lib.lib().lbvh_batch_create(self.ctx.handle, ctypes.byref(h)))
+        self._h = h
+        self._keep = None
+        self.offsets = None
+
+    def build(self, triangles, offsets) -> "Batch":
+        offsets = _u32(offsets, "offsets")
+        n_meshes = (offsets.size if isinstance(offsets, np.ndarray) else offsets.numel()) - 1
+        total = _rows(triangles, 12, "triangles")
+        if n_meshes < 1:
+            raise ValueError("need at least one mesh")
+        self.ctx.check(_lib.lib().lbvh_batch_build_triangles(self.ctx.handle, _addr(triangles), total,
+                                                            _addr(offsets), n_meshes, self._h))
+        self._keep = (triangles, offsets)
+        self.offsets = offsets if isinstance(offsets, np.ndarray) else offsets.cpu().numpy().view(np.uint32)
+        return self
+
+    def info(self):
+        a, b, c = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        _lib.lib().lbvh_batch_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def nodes(self, out=None):
+        """All node blocks (NODE_DTYPE); mesh k's block starts at offsets[k] - k."""
+        if out is None:
+            out = np.empty(self.info()[2], NODE_DTYPE)
+        self.ctx.check(_lib.lib().lbvh_batch_nodes(self.ctx.handle, self._h, _addr(out)))
+        return out
+
+    def mesh_nodes(self, k: int, all_nodes=None):
+        nodes = self.nodes() if all_nodes is None else all_nodes
+        o = self.offsets
+        start = int(o[k]) - k
+        return nodes[start : start + int(o[k + 1] - o[k]) - 1]
+
+    def trace(self, rays, ray_offsets, out=None):
+        """rays [m, 8]; rays [ray_offsets[k], ray_offsets[k + 1]) hit mesh k."""
+        ray_offsets = _u32(ray_offsets, "ray_offsets")
+        m = _rows(rays, 8, "rays")
+        if out is None:
+            if _is_cuda(rays):
+                out = torch.empty((m, 4), dtype=torch.float32, device=rays.device)
+            else:
+                out = np.empty(m, HIT_DTYPE)
+        self.ctx.check(_lib.lib().lbvh_batch_trace_triangles(self.ctx.handle, self._h, _addr(rays),
+                                                            _addr(ray_offsets), m, _addr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lib().lbvh_batch_destroy(self.ctx.handle, self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

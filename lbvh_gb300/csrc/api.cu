@@ -3,6 +3,7 @@
 // lbvh::builder<float>, lbvh::bvh<float> and lbvh::traverser.
 #include "../../include/lbvh_gb300.h"
 
+#include "batch.cuh"
 #include "build.cuh"
 #include "trace.cuh"
 
@@ -47,6 +48,8 @@ struct lbvh_ctx
   DevBuf prims_in;             // staging for host refit input
   uint32_t* ray_counter = nullptr; // persistent-trace ray dispenser
   TraceParams trace;               // traversal launch shape
+  uint32_t batch_threads = 512;    // CTA size of the batched build
+  DevBuf batch_ws;                 // batched build: codes, boxes, slots
   uint32_t epoch = 0;          // look-back epoch of the last sort pass
   char msg[512] = { 0 };
 };
@@ -474,6 +477,7 @@ lbvh_ctx_destroy(lbvh_ctx* c)
   release(c->ws, c->stream);
   release(c->slots, c->stream);
   release(c->lookback, c->stream);
+  release(c->batch_ws, c->stream);
   release(c->rays, c->stream);
   release(c->hits, c->stream);
   release(c->counts, c->stream);
@@ -530,6 +534,12 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
       if (value < 1 || value > 32)
         return fail(c, LBVH_ERR_INVALID_ARG, "trace blocks per SM %d outside [1, 32]", value);
       c->trace.blocks_per_sm = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_BATCH_THREADS:
+      if (value < 256 || value > kBatchMaxThreads || value % 32)
+        return fail(c, LBVH_ERR_INVALID_ARG, "batch CTA size %d: a multiple of 32 in [256, %d]", value,
+                    kBatchMaxThreads);
+      c->batch_threads = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_TRACE_REFILL:
       if (value < 1 || value > 32)
@@ -804,6 +814,207 @@ lbvh_trace_triangles_counts(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, s
   if (!n_box || !n_tri)
     return fail(c, LBVH_ERR_INVALID_ARG, "null count output");
   return trace_common(c, b, rays, m, hits, n_box, n_tri);
+}
+
+} // extern "C"
+
+// ---------------------------------------------------------------------------
+// batched meshes
+
+struct lbvh_batch
+{
+  int device = 0;
+  uint32_t n_meshes = 0;
+  uint32_t total = 0;
+  DevBuf off;                // device copy of the n_meshes + 1 offsets
+  const void* tris = nullptr;
+  DevBuf tris_owned;
+  DevBuf nodes;              // total - n_meshes nodes
+  DevBuf wnodes;             // traversal copy + flag word
+  bool wnodes_valid = false;
+  DevBuf roff;               // device copy of the ray offsets
+};
+
+namespace {
+
+// Validates offsets on the host when they live there (exact error), else
+// leaves it to the device check (reported at the next synchronization).
+int
+host_offsets_ok(lbvh_ctx* c, const uint32_t* off, size_t n_meshes, size_t total, size_t min_count)
+{
+  if (on_device(off))
+    return LBVH_OK;
+  if (off[0] != 0 || off[n_meshes] != total)
+    return fail(c, LBVH_ERR_INVALID_ARG, "offsets must start at 0 and end at the total (%zu)", total);
+  for (size_t k = 0; k < n_meshes; k++)
+    if (off[k + 1] < off[k] || off[k + 1] - off[k] < min_count)
+      return fail(c, LBVH_ERR_INVALID_ARG, "segment %zu has %u items (at least %zu needed)", k,
+                  off[k + 1] < off[k] ? 0u : off[k + 1] - off[k], min_count);
+  return LBVH_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int
+lbvh_batch_create(lbvh_ctx* c, lbvh_batch** out)
+{
+  if (!c || !out)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  *out = new (std::nothrow) lbvh_batch;
+  if (!*out)
+    return fail(c, LBVH_ERR_OOM, "host allocation failed");
+  (*out)->device = c->device;
+  return LBVH_OK;
+}
+
+int
+lbvh_batch_destroy(lbvh_ctx* c, lbvh_batch* b)
+{
+  if (!c || !b)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  set_device(c);
+  release(b->off, c->stream);
+  release(b->tris_owned, c->stream);
+  release(b->nodes, c->stream);
+  release(b->wnodes, c->stream);
+  release(b->roff, c->stream);
+  delete b;
+  return LBVH_OK;
+}
+
+int
+lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const uint32_t* offsets, size_t n_meshes,
+                           lbvh_batch* b)
+{
+  if (!c || !tris || !offsets || !b)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (n_meshes < 1 || total < 2 * n_meshes || total > kMaxPrims)
+    return fail(c, LBVH_ERR_INVALID_ARG, "%zu meshes over %zu triangles", n_meshes, total);
+  int st = set_device(c);
+  if (st)
+    return st;
+  if ((st = host_offsets_ok(c, offsets, n_meshes, total, 2)))
+    return st;
+  const bool host = !on_device(tris);
+  CK(reserve(b->off, 4 * (n_meshes + 1), c->stream), "offset allocation");
+  CK(cudaMemcpyAsync(b->off.ptr, offsets, 4 * (n_meshes + 1), cudaMemcpyDefault, c->stream), "offset upload");
+  const void* dt = tris;
+  if (host) {
+    CK(reserve(b->tris_owned, sizeof(Tri) * total, c->stream), "primitive allocation");
+    CK(cudaMemcpyAsync(b->tris_owned.ptr, tris, sizeof(Tri) * total, cudaMemcpyHostToDevice, c->stream),
+       "primitive upload");
+    dt = b->tris_owned.ptr;
+  } else if (reinterpret_cast<uintptr_t>(tris) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device triangles must be 16-byte aligned");
+  }
+  CK(reserve(b->nodes, sizeof(Node) * (total - n_meshes), c->stream), "node allocation");
+  CK(reserve(c->batch_ws, 36 * total + 1024, c->stream), "batch workspace allocation");
+  char* ws = static_cast<char*>(c->batch_ws.ptr);
+  BatchBuffers bb{};
+  bb.off = static_cast<const uint32_t*>(b->off.ptr);
+  bb.n_meshes = uint32_t(n_meshes);
+  bb.total = uint32_t(total);
+  bb.queue = c->ray_counter + 8;
+  bb.keys_a = reinterpret_cast<uint32_t*>(ws);
+  bb.keys_b = bb.keys_a + total;
+  bb.slots = bb.keys_b + total;
+  bb.boxes = reinterpret_cast<Box*>(bb.slots + total);
+  bb.error = &c->state->error;
+  CK(launch_batch_build(static_cast<const Tri*>(dt), bb, static_cast<Node*>(b->nodes.ptr), c->batch_threads,
+                        c->num_sms, c->stream),
+     "batch build launch");
+  b->n_meshes = uint32_t(n_meshes);
+  b->total = uint32_t(total);
+  b->tris = dt;
+  b->device = c->device;
+  b->wnodes_valid = false;
+  return host ? check_device(c) : LBVH_OK;
+}
+
+int
+lbvh_batch_info(const lbvh_batch* b, size_t* n_meshes, size_t* total_prims, size_t* total_nodes)
+{
+  if (!b)
+    return LBVH_ERR_INVALID_ARG;
+  if (n_meshes)
+    *n_meshes = b->n_meshes;
+  if (total_prims)
+    *total_prims = b->total;
+  if (total_nodes)
+    *total_nodes = b->total - b->n_meshes;
+  return LBVH_OK;
+}
+
+int
+lbvh_batch_nodes(lbvh_ctx* c, const lbvh_batch* b, void* dst)
+{
+  if (!c || !b || !dst)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (!b->n_meshes)
+    return fail(c, LBVH_ERR_INVALID_ARG, "batch has not been built");
+  int st = set_device(c);
+  if (st)
+    return st;
+  const bool host = !on_device(dst);
+  CK(cudaMemcpyAsync(dst, b->nodes.ptr, sizeof(Node) * (b->total - b->n_meshes), cudaMemcpyDefault, c->stream),
+     "node copy");
+  return host ? check_device(c) : LBVH_OK;
+}
+
+int
+lbvh_batch_trace_triangles(lbvh_ctx* c, const lbvh_batch* b, const float* rays, const uint32_t* ray_offsets, size_t m,
+                           void* hits)
+{
+  if (!c || !b || !ray_offsets || (m && (!rays || !hits)))
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (!b->n_meshes)
+    return fail(c, LBVH_ERR_INVALID_ARG, "batch has not been built");
+  if (m > 0x7fffffffull)
+    return fail(c, LBVH_ERR_INVALID_ARG, "ray count %zu too large", m);
+  int st = set_device(c);
+  if (st)
+    return st;
+  if ((st = host_offsets_ok(c, ray_offsets, b->n_meshes, m, 0)))
+    return st;
+  if (m == 0)
+    return LBVH_OK;
+  lbvh_batch* mb = const_cast<lbvh_batch*>(b); // traversal copy and offsets are caches
+  const uint32_t total_nodes = b->total - b->n_meshes;
+  if (!mb->wnodes_valid) {
+    CK(reserve(mb->wnodes, sizeof(WideNode) * (total_nodes + 1), c->stream), "traversal layout allocation");
+    CK(launch_batch_repack(static_cast<const Node*>(b->nodes.ptr), total_nodes, static_cast<const uint32_t*>(b->off.ptr),
+                           b->n_meshes, static_cast<WideNode*>(mb->wnodes.ptr), c->stream),
+       "repack launch");
+    mb->wnodes_valid = true;
+  }
+  CK(reserve(mb->roff, 4 * (b->n_meshes + 1), c->stream), "ray offset allocation");
+  CK(cudaMemcpyAsync(mb->roff.ptr, ray_offsets, 4 * (b->n_meshes + 1), cudaMemcpyDefault, c->stream),
+     "ray offset upload");
+  const bool hr = !on_device(rays), hh = !on_device(hits);
+  const float* dr = rays;
+  Hit* dh = static_cast<Hit*>(hits);
+  if (hr) {
+    CK(reserve(c->rays, 32 * m, c->stream), "ray staging allocation");
+    CK(cudaMemcpyAsync(c->rays.ptr, rays, 32 * m, cudaMemcpyHostToDevice, c->stream), "ray upload");
+    dr = static_cast<const float*>(c->rays.ptr);
+  } else if (reinterpret_cast<uintptr_t>(rays) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device rays must be 16-byte aligned");
+  }
+  if (hh) {
+    CK(reserve(c->hits, 16 * m, c->stream), "hit staging allocation");
+    dh = static_cast<Hit*>(c->hits.ptr);
+  } else if (reinterpret_cast<uintptr_t>(hits) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device hits must be 16-byte aligned");
+  }
+  CK(launch_batch_trace(static_cast<const WideNode*>(mb->wnodes.ptr), total_nodes, static_cast<const Tri*>(b->tris),
+                        static_cast<const uint32_t*>(b->off.ptr), static_cast<const uint32_t*>(mb->roff.ptr),
+                        b->n_meshes, dr, uint32_t(m), dh, c->ray_counter, c->num_sms, c->trace, c->stream),
+     "batch trace launch");
+  if (hh)
+    CK(cudaMemcpyAsync(hits, dh, 16 * m, cudaMemcpyDeviceToHost, c->stream), "hit download");
+  return (hr || hh) ? check_device(c) : LBVH_OK;
 }
 
 } // extern "C"

@@ -1,0 +1,52 @@
+// Batched build + trace of many independent meshes.
+#pragma once
+
+#include "build.cuh"
+#include "trace.cuh"
+
+namespace lbvh_gb300 {
+
+constexpr int kBatchItems = 4;         // keys per thread per sort chunk
+constexpr int kBatchMaxThreads = 1024; // largest CTA of the batched build
+
+// Device views for one batched build of n_meshes meshes, total triangles.
+// Mesh m owns triangles [off[m], off[m + 1]) and nodes
+// [off[m] - m, off[m + 1] - m - 1): its node block is exactly the node array
+// the reference builds for that mesh alone (local child indices).
+struct BatchBuffers
+{
+  const uint32_t* off;        // n_meshes + 1 triangle offsets
+  uint32_t n_meshes;
+  uint32_t total;             // off[n_meshes]: all triangles
+  uint32_t* queue;            // mesh dispenser (zeroed before the launch)
+  uint32_t* keys_a;           // total
+  uint32_t* keys_b;           // total
+  Box* boxes;                 // total leaf boxes
+  uint32_t* slots;            // total arrival slots (cleared per mesh)
+  uint32_t* error;            // sticky kErr* bits
+};
+
+cudaError_t launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t threads, int num_sms,
+                               cudaStream_t s);
+
+// Traversal copy of every mesh's nodes (local child references), plus the
+// scene-bound flag word after the last node.
+cudaError_t launch_batch_repack(const Node* nodes, uint32_t total_nodes, const uint32_t* off, uint32_t n_meshes,
+                                WideNode* out, cudaStream_t s);
+
+// Rays [roff[m], roff[m + 1]) are traced against mesh m.
+cudaError_t launch_batch_trace(const WideNode* wnodes,
+                               uint32_t total_nodes,
+                               const Tri* tris,
+                               const uint32_t* off,
+                               const uint32_t* roff,
+                               uint32_t n_meshes,
+                               const float* rays,
+                               uint32_t m,
+                               Hit* hits,
+                               uint32_t* ray_counter,
+                               int num_sms,
+                               const TraceParams& p,
+                               cudaStream_t s);
+
+} // namespace lbvh_gb300

@@ -6,6 +6,7 @@
 // Every kernel reproduces the reference's outputs bit for bit; the comments on
 // each kernel cite the reference code it replaces.
 #include "build.cuh"
+#include "device_util.cuh"
 
 #include <atomic>
 
@@ -47,90 +48,6 @@ k_make_triangles(const float* __restrict__ verts, uint32_t n, Tri* __restrict__ 
 // the lower index on compare-equal values, which gives the same winner for
 // any reduction tree. Accumulators start at +/-inf and only take a candidate
 // on a strict comparison, so NaN never enters, as in the reference.
-
-struct ArgBox
-{
-  float v[6];
-  uint32_t i[6];
-};
-
-__device__ __forceinline__ void
-take_lo(float& v, uint32_t& i, float v2, uint32_t i2)
-{
-  if (v2 < v || (!(v < v2) && i2 < i)) {
-    v = v2;
-    i = i2;
-  }
-}
-__device__ __forceinline__ void
-take_hi(float& v, uint32_t& i, float v2, uint32_t i2)
-{
-  if (v < v2 || (!(v2 < v) && i2 < i)) {
-    v = v2;
-    i = i2;
-  }
-}
-
-__device__ __forceinline__ void
-combine(ArgBox& a, const ArgBox& b)
-{
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-    take_lo(a.v[k], a.i[k], b.v[k], b.i[k]);
-#pragma unroll
-  for (int k = 3; k < 6; k++)
-    take_hi(a.v[k], a.i[k], b.v[k], b.i[k]);
-}
-
-__device__ __forceinline__ ArgBox
-empty_arg()
-{
-  ArgBox a;
-  const float inf = __int_as_float(0x7f800000);
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    a.v[k] = inf;
-    a.v[k + 3] = -inf;
-  }
-#pragma unroll
-  for (int k = 0; k < 6; k++)
-    a.i[k] = 0xffffffffu;
-  return a;
-}
-
-__device__ __forceinline__ ArgBox
-block_reduce_arg(ArgBox a, ArgBox* s_part)
-{
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    ArgBox b;
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-      b.v[k] = __shfl_down_sync(0xffffffffu, a.v[k], o);
-      b.i[k] = __shfl_down_sync(0xffffffffu, a.i[k], o);
-    }
-    combine(a, b);
-  }
-  if (lane == 0)
-    s_part[warp] = a;
-  __syncthreads();
-  if (warp == 0) {
-    const int nw = blockDim.x >> 5;
-    a = lane < nw ? s_part[lane] : empty_arg();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ArgBox b;
-#pragma unroll
-      for (int k = 0; k < 6; k++) {
-        b.v[k] = __shfl_down_sync(0xffffffffu, a.v[k], o);
-        b.i[k] = __shfl_down_sync(0xffffffffu, a.i[k], o);
-      }
-      combine(a, b);
-    }
-  }
-  return a; // valid in thread 0
-}
 
 template<class Leaf>
 __global__ __launch_bounds__(kBoundsThreads) void
@@ -493,31 +410,6 @@ k_onesweep(const uint32_t* __restrict__ kin,
 // after one, only when that child is an internal node; leaf boxes are
 // recomputed from the primitives.
 
-__device__ __forceinline__ int
-boundary_delta(const uint32_t* __restrict__ codes, uint32_t n, uint32_t k)
-{
-  if (k >= n - 1) // k = L - 1 wraps for L = 0; k = n - 1 is past the end
-    return -1;
-  const uint32_t a = __ldg(codes + k), b = __ldg(codes + k + 1);
-  return a == b ? int(__clz(k ^ (k + 1))) + 32 : int(__clz(a ^ b));
-}
-
-__device__ __forceinline__ void
-store_node(Node* __restrict__ nodes, uint32_t idx, const Box& b, uint32_t l, uint32_t r)
-{
-  float4* dst = reinterpret_cast<float4*>(nodes + idx);
-  __stcg(dst + 0, make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]));
-  __stcg(dst + 1, make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r)));
-}
-
-__device__ __forceinline__ Box
-load_node_box(const Node* __restrict__ nodes, uint32_t idx)
-{
-  const float4 a = __ldcg(reinterpret_cast<const float4*>(nodes + idx));
-  const float2 b = __ldcg(reinterpret_cast<const float2*>(nodes + idx) + 2);
-  return Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
-}
-
 // Two phases.
 //
 // Local phase (k_tree_local), one CTA per kTreeBlock consecutive leaf slots:
@@ -547,18 +439,6 @@ static_assert(sizeof(PendingNode) == 32, "pending record layout");
 
 constexpr uint32_t kSlotEmpty = 0xffffffffu;    // no arrival yet
 constexpr uint32_t kSlotComplete = 0xfffffffeu; // both children arrived
-
-__device__ __forceinline__ void
-stage_record(Node& rec, const Box& b, uint32_t l, uint32_t r)
-{
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    rec.lo[k] = b.lo[k];
-    rec.hi[k] = b.hi[k];
-  }
-  rec.left = l;
-  rec.right = r;
-}
 
 template<class Leaf>
 __global__ __launch_bounds__(kTreeThreads) void

@@ -20,6 +20,7 @@
 //     its warp's batch (ballot + shuffle), and a warp fetches a new batch of
 //     32 rays with one atomic, so lanes do not idle while the longest ray of
 //     a fixed group finishes.
+#include "batch.cuh"
 #include "trace.cuh"
 
 namespace lbvh_gb300 {
@@ -157,7 +158,9 @@ k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict_
 
 // ---------------------------------------------------------------------------
 
-template<bool kCounts>
+// kBatch: rays [roff[k], roff[k + 1]) belong to mesh k, whose nodes start at
+// moff[k] - k and whose triangles start at moff[k] (local indices inside).
+template<bool kCounts, bool kBatch>
 __global__ __launch_bounds__(kTraceThreads) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
@@ -169,7 +172,10 @@ k_trace(const WideNode* __restrict__ wnodes,
         uint32_t* __restrict__ n_tri,
         uint32_t* __restrict__ ray_counter,
         const uint32_t* __restrict__ wide,
-        uint32_t refill)
+        uint32_t refill,
+        const uint32_t* __restrict__ moff,
+        const uint32_t* __restrict__ roff,
+        uint32_t n_meshes)
 {
   const bool scene_fast = __ldg(wide) == 0;
   const uint32_t lane = threadIdx.x & 31;
@@ -189,6 +195,7 @@ k_trace(const WideNode* __restrict__ wnodes,
   uint32_t best_p = kMiss;
   float best_t = inf, best_u = 0.0f, best_v = 0.0f;
   uint32_t cb = 0, ct = 0;
+  uint32_t nb = 0, tb = 0; // batched: the ray's mesh node and triangle bases
 
   // the warp's current batch of 32 ray ids (warp-uniform state)
   uint32_t batch = 0, batch_left = 0;
@@ -231,6 +238,18 @@ k_trace(const WideNode* __restrict__ wnodes,
             ray = id;
             r = make_ray(__ldg(rays + 2 * size_t(id)), __ldg(rays + 2 * size_t(id) + 1));
             r.fast = r.fast && scene_fast;
+          if (kBatch) { // the mesh k with roff[k] <= id < roff[k + 1]
+            uint32_t lo = 0, hi = n_meshes; // invariant: roff[lo] <= id < roff[hi]
+            while (hi - lo > 1) {
+              const uint32_t mid = (lo + hi) >> 1;
+              if (__ldg(roff + mid) <= id)
+                lo = mid;
+              else
+                hi = mid;
+            }
+            tb = __ldg(moff + lo);
+            nb = tb - lo;
+          }
             sp = 0;
             cur = make_uint2(0u, __float_as_uint(inf)); // root, pushed with +inf
             has_cur = true;
@@ -247,7 +266,7 @@ k_trace(const WideNode* __restrict__ wnodes,
 
     // ---- one node visit (lbvh.h:1902-1938); cur passed the cull test ----
     {
-      const float4* w = reinterpret_cast<const float4*>(wnodes + cur.x);
+      const float4* w = reinterpret_cast<const float4*>(wnodes + nb + cur.x);
       const float4 A = __ldg(w + 0), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
       const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
       bool lhit = false, rhit = false;
@@ -271,7 +290,7 @@ k_trace(const WideNode* __restrict__ wnodes,
           float t, u, v;
           if (kCounts)
             ct++;
-          if (tri_test(r, tris, p, t, u, v) && t < best_t) {
+          if (tri_test(r, tris + tb, p, t, u, v) && t < best_t) {
             best_p = p;
             best_t = t;
             best_u = u;
@@ -364,11 +383,102 @@ launch_trace_tris(const WideNode* wnodes,
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + n_nodes);
   if (n_box && n_tri)
-    k_trace<true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri, ray_counter,
-                                                   wide, p.refill);
+    k_trace<true, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri,
+                                                          ray_counter, wide, p.refill, nullptr, nullptr, 0);
   else
-    k_trace<false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
-                                                    ray_counter, wide, p.refill);
+    k_trace<false, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
+                                                           ray_counter, wide, p.refill, nullptr, nullptr, 0);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// batched meshes (launch_batch_repack / launch_batch_trace, batch.cuh)
+
+__global__ void
+k_batch_repack(const Node* __restrict__ nodes,
+               uint32_t total_nodes,
+               const uint32_t* __restrict__ off,
+               uint32_t n_meshes,
+               WideNode* __restrict__ out,
+               uint32_t* __restrict__ wide)
+{
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= total_nodes)
+    return;
+  // the mesh k with off[k] - k <= g < off[k + 1] - (k + 1)
+  uint32_t lo = 0, hi = n_meshes;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) - mid <= g)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const uint32_t base = __ldg(off + lo) - lo;
+  const uint32_t nn = __ldg(off + lo + 1) - __ldg(off + lo) - 1; // the mesh's internal nodes
+  const float4* nv = reinterpret_cast<const float4*>(nodes + base);
+  const uint32_t i = g - base;
+  const float4 self = __ldg(nv + 2 * size_t(i) + 1);
+  const uint32_t l = __float_as_uint(self.z), r = __float_as_uint(self.w);
+  float4 la = make_float4(0, 0, 0, 0), lb = la, ra = la, rb = la;
+  if (!(l & kLeafBit) && l < nn) {
+    la = __ldg(nv + 2 * size_t(l));
+    lb = __ldg(nv + 2 * size_t(l) + 1);
+  }
+  if (!(r & kLeafBit) && r < nn) {
+    ra = __ldg(nv + 2 * size_t(r));
+    rb = __ldg(nv + 2 * size_t(r) + 1);
+  }
+  if (!bounded(la) || !bounded(make_float4(lb.x, lb.y, ra.x, ra.y)) || !bounded(make_float4(ra.z, ra.w, rb.x, rb.y)))
+    atomicOr(wide, 1u);
+  WideNode w;
+  w.a = make_float4(la.x, la.y, la.z, la.w);
+  w.b = make_float4(lb.x, lb.y, ra.x, ra.y);
+  w.c = make_float4(ra.z, ra.w, rb.x, rb.y);
+  w.d = make_float4(__uint_as_float(l), __uint_as_float(r), 0.0f, 0.0f);
+  out[g] = w;
+}
+
+cudaError_t
+launch_batch_repack(const Node* nodes, uint32_t total_nodes, const uint32_t* off, uint32_t n_meshes, WideNode* out,
+                    cudaStream_t s)
+{
+  uint32_t* wide = reinterpret_cast<uint32_t*>(out + total_nodes);
+  cudaError_t e = cudaMemsetAsync(wide, 0, 4, s);
+  if (e != cudaSuccess)
+    return e;
+  if (total_nodes)
+    k_batch_repack<<<ceil_div_u32(total_nodes, 256), 256, 0, s>>>(nodes, total_nodes, off, n_meshes, out, wide);
+  return cudaGetLastError();
+}
+
+cudaError_t
+launch_batch_trace(const WideNode* wnodes,
+                   uint32_t total_nodes,
+                   const Tri* tris,
+                   const uint32_t* off,
+                   const uint32_t* roff,
+                   uint32_t n_meshes,
+                   const float* rays,
+                   uint32_t m,
+                   Hit* hits,
+                   uint32_t* ray_counter,
+                   int num_sms,
+                   const TraceParams& p,
+                   cudaStream_t s)
+{
+  if (m == 0)
+    return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(ray_counter, 0, 4, s);
+  if (e != cudaSuccess)
+    return e;
+  const uint32_t want = ceil_div_u32(m, kTraceThreads);
+  const uint32_t cap = uint32_t(num_sms) * p.blocks_per_sm;
+  const uint32_t blocks = want < cap ? want : cap;
+  const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + total_nodes);
+  k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, nullptr, reinterpret_cast<const float4*>(rays),
+                                                        m, hits, nullptr, nullptr, ray_counter, wide, p.refill, off,
+                                                        roff, n_meshes);
   return cudaGetLastError();
 }
 

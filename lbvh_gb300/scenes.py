@@ -351,3 +351,21 @@ def random_rays_in_box(lo, hi, m: int, seed: int, stream: int = 70, scale: float
     h = 0.5 * (hi - lo) * scale
     o = c + (uniform(seed, stream, 3 * m).reshape(m, 3) * 2.0 - 1.0) * h
     return _rays(o, sphere_dirs(seed, stream + 1, m))
+
+
+def batch_scene(k: int = 4096, lo: int = 64, hi: int = 65536, rays_per_mesh: int = 4096, seed: int = 3):
+    """Batched workload: k independent random-order soups (each as
+    soup_vertices, centroids uniform in [-1, 1]^3, drawn with its own seed
+    base + i) with triangle counts log-uniform in [lo, hi], concatenated,
+    and rays_per_mesh random rays per mesh (origins uniform in the 1.5x box of
+    the soups' common extent, directions uniform on the sphere).
+    Returns (triangles [total, 12], offsets [k + 1] uint32, rays, ray_offsets)."""
+    counts = log_uniform_counts(k, lo, hi, seed)
+    offsets = np.zeros(k + 1, np.uint32)
+    offsets[1:] = np.cumsum(counts)
+    tris = np.empty((int(offsets[-1]), 12), np.float32)
+    for i in range(k):
+        tris[offsets[i] : offsets[i + 1]] = soup_large(int(counts[i]), seed * 1_000_003 + i)
+    rays = random_rays_in_box([-1.0] * 3, [1.0] * 3, k * rays_per_mesh, seed, stream=80)
+    ray_offsets = (np.arange(k + 1, dtype=np.int64) * rays_per_mesh).astype(np.uint32)
+    return tris, offsets, rays, ray_offsets
