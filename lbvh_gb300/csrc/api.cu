@@ -910,17 +910,22 @@ lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const u
     return fail(c, LBVH_ERR_INVALID_ARG, "device triangles must be 16-byte aligned");
   }
   CK(reserve(b->nodes, sizeof(Node) * (total - n_meshes), c->stream), "node allocation");
-  CK(reserve(c->batch_ws, 36 * total + 1024, c->stream), "batch workspace allocation");
+  // every array on a 256-byte boundary (the boxes are read as 8-byte pairs)
+  const size_t o_keys_a = align_up(24 * total, 256);
+  const size_t o_keys_b = o_keys_a + align_up(4 * total, 256);
+  const size_t o_slots = o_keys_b + align_up(4 * total, 256);
+  const size_t ws_bytes = o_slots + align_up(4 * total, 256);
+  CK(reserve(c->batch_ws, ws_bytes, c->stream), "batch workspace allocation");
   char* ws = static_cast<char*>(c->batch_ws.ptr);
   BatchBuffers bb{};
   bb.off = static_cast<const uint32_t*>(b->off.ptr);
   bb.n_meshes = uint32_t(n_meshes);
   bb.total = uint32_t(total);
   bb.queue = c->ray_counter + 8;
-  bb.keys_a = reinterpret_cast<uint32_t*>(ws);
-  bb.keys_b = bb.keys_a + total;
-  bb.slots = bb.keys_b + total;
-  bb.boxes = reinterpret_cast<Box*>(bb.slots + total);
+  bb.boxes = reinterpret_cast<Box*>(ws);
+  bb.keys_a = reinterpret_cast<uint32_t*>(ws + o_keys_a);
+  bb.keys_b = reinterpret_cast<uint32_t*>(ws + o_keys_b);
+  bb.slots = reinterpret_cast<uint32_t*>(ws + o_slots);
   bb.error = &c->state->error;
   CK(launch_batch_build(static_cast<const Tri*>(dt), bb, static_cast<Node*>(b->nodes.ptr), c->batch_threads,
                         c->num_sms, c->stream),
