@@ -201,6 +201,106 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
                          "traffic": None, "peak_kind": peak_kind}}
 
 
+def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_per_mesh=4096, seed=3):
+    """Batched workload: n_meshes soups with log-uniform [64, 65,536]
+    triangles and rays_per_mesh random rays each. Build + trace of all meshes
+    in one persistent launch each, tuned by the autotuner and replayed as a
+    CUDA graph, against the plain path (one build + one trace call per mesh)."""
+    import torch
+
+    import lbvh_gb300 as lb
+    from lbvh_gb300 import autotune, scenes
+
+    dev = torch.device("cuda", ctx_device)
+    tris_h, off_h, rays_h, roff_h = scenes.batch_scene(n_meshes, 64, 65536, rays_per_mesh, seed)
+    tris = torch.from_numpy(tris_h).to(dev)
+    rays = torch.from_numpy(rays_h).to(dev)
+    off = torch.from_numpy(off_h.view(np.int32)).to(dev)
+    roff = torch.from_numpy(roff_h.view(np.int32)).to(dev)
+    del tris_h, rays_h
+    out = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    s = torch.cuda.Stream(dev)
+    ctx = lb.Context(ctx_device, s.cuda_stream)
+    res = {"meshes": n_meshes, "triangles": int(off_h[-1]), "rays": int(rays.shape[0]),
+           "workload": f"batch{n_meshes}_loguniform64-65536_{rays_per_mesh}rays"}
+    with torch.cuda.stream(s):
+        setting = autotune.tune_batch(ctx, tris, off, rays, roff, key=f"gb300:{res['workload']}")
+        res["tuning"] = {k: setting[k] for k in ("batch_threads", "trace_blocks_per_sm", "trace_refill")}
+        batch = lb.Batch(ctx)
+        for _ in range(3):
+            batch.build(tris, off)
+            batch.trace(rays, roff, out=out)
+        torch.cuda.synchronize()
+        ref_out = out.clone()
+        bt, tt = [], []
+        for _ in range(max(3, min(steps, 10))):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(s)
+            batch.build(tris, off)
+            e[1].record(s)
+            batch.trace(rays, roff, out=out)
+            e[2].record(s)
+            torch.cuda.synchronize()
+            bt.append(e[0].elapsed_time(e[1]))
+            tt.append(e[1].elapsed_time(e[2]))
+        ctx.synchronize()
+        assert torch.equal(out.view(torch.int32), ref_out.view(torch.int32))
+    build_ms, trace_ms = float(np.mean(bt)), float(np.mean(tt))
+    res.update({"build_ms": round(build_ms, 3), "trace_ms": round(trace_ms, 3),
+                "step_ms": round(build_ms + trace_ms, 3),
+                "build_mprims_s": round(res["triangles"] / (build_ms * 1e-3) / 1e6, 1),
+                "trace_mrays_s": round(res["rays"] / (trace_ms * 1e-3) / 1e6, 1),
+                "gpu_launches_per_step": 5})
+    # the same step captured once as a CUDA graph and replayed
+    try:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+            batch.build(tris, off)
+            batch.trace(rays, roff, out=out)
+        gt = []
+        for _ in range(max(3, min(steps, 10))):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                a.record(s)
+                g.replay()
+                b.record(s)
+            torch.cuda.synchronize()
+            gt.append(a.elapsed_time(b))
+        assert torch.equal(out.view(torch.int32), ref_out.view(torch.int32))
+        res["graph_step_ms"] = round(float(np.mean(gt)), 3)
+    except Exception as exc:  # capture is an optimisation: report why it was skipped
+        res["graph_step_ms"] = None
+        res["graph_error"] = str(exc)[:200]
+    # plain path: one build + one trace call per mesh on the same data
+    with torch.cuda.stream(s):
+        builder = lb.Builder(ctx)
+        bvh = lb.BVH(ctx)
+        hits = torch.empty((rays_per_mesh, 4), dtype=torch.float32, device=dev)
+        ctx.reserve(65536, 0)
+        for k in range(8):  # warm-up
+            builder(tris[off_h[k]:off_h[k + 1]], into=bvh)
+            lb.Traverser(bvh)(rays[roff_h[k]:roff_h[k + 1]], out=hits)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for k in range(n_meshes):
+            builder(tris[off_h[k]:off_h[k + 1]], into=bvh)
+            lb.Traverser(bvh)(rays[roff_h[k]:roff_h[k + 1]], out=hits)
+        b.record(s)
+        torch.cuda.synchronize()
+        plain_ms = max(a.elapsed_time(b), 1e3 * (time.perf_counter() - t0))
+    res["plain_step_ms"] = round(plain_ms, 3)
+    best = res["graph_step_ms"] or res["step_ms"]
+    res["speedup_vs_plain"] = round(plain_ms / best, 2)
+    del tris, rays, out, flush
+    torch.cuda.empty_cache()
+    return res
+
+
 # --------------------------------------------------------------------------
 # our arm
 
@@ -214,6 +314,8 @@ def main():
     ap.add_argument("--no-16m", action="store_true", help="skip the 16M-triangle build measurement")
     ap.add_argument("--only-16m", action="store_true", help="only the 16M-triangle build (profiling)")
     ap.add_argument("--soup-n", type=int, default=N_BUILD_16M, help="soup size of the build measurement")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
+    ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -236,6 +338,12 @@ def main():
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     ctx = lb.Context(local, stream.cuda_stream)
+
+    if args.only_batched:
+        r = measure_batched(local, args.steps, hbm_peak, peak_kind)
+        if rank == 0:
+            print(json.dumps({"batched": r}), flush=True)
+        return 0
 
     if args.only_16m:
         flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
@@ -343,6 +451,11 @@ def main():
         build_16m = measure_build_16m(ctx, builder, stream, flush, dev, args.steps, hbm_peak, peak_kind,
                                       args.soup_n)
 
+    # ---- batched meshes (4,096 soups) vs the plain per-mesh path ----------
+    batched = None
+    if not args.no_batched:
+        batched = measure_batched(local, args.steps, hbm_peak, peak_kind)
+
     # ---- CPU baseline: the oracle port (or reference) on the host cores ---
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -377,6 +490,7 @@ def main():
         "trace": {"ms": round(trace_mean, 4), "mrays_s": round(m / (trace_mean * 1e-3) / 1e6, 1),
                   "hit_fraction": round(hit_frac, 4)},
         "build_16m": build_16m,
+        "batched": batched,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
