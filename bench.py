@@ -281,15 +281,15 @@ def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_
         hits = torch.empty((rays_per_mesh, 4), dtype=torch.float32, device=dev)
         ctx.reserve(65536, 0)
         for k in range(8):  # warm-up
-            builder(tris[off_h[k]:off_h[k + 1]], into=bvh)
-            lb.Traverser(bvh)(rays[roff_h[k]:roff_h[k + 1]], out=hits)
+            builder(tris[int(off_h[k]):int(off_h[k + 1])], into=bvh)
+            lb.Traverser(bvh)(rays[int(roff_h[k]):int(roff_h[k + 1])], out=hits)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(s)
         for k in range(n_meshes):
-            builder(tris[off_h[k]:off_h[k + 1]], into=bvh)
-            lb.Traverser(bvh)(rays[roff_h[k]:roff_h[k + 1]], out=hits)
+            builder(tris[int(off_h[k]):int(off_h[k + 1])], into=bvh)
+            lb.Traverser(bvh)(rays[int(roff_h[k]):int(roff_h[k + 1])], out=hits)
         b.record(s)
         torch.cuda.synchronize()
         plain_ms = max(a.elapsed_time(b), 1e3 * (time.perf_counter() - t0))

@@ -382,7 +382,8 @@ class Batch:
         self.ctx.check(_lib.lib().lbvh_batch_create(self.ctx.handle, ctypes.byref(h)))
         self._h = h
         self._keep = None
-        self.offsets = None
+        self._offsets = None
+        self._offsets_host = None
 
     def build(self, triangles, offsets) -> "Batch":
         offsets = _u32(offsets, "offsets")
@@ -393,8 +394,16 @@ class Batch:
         self.ctx.check(_lib.lib().lbvh_batch_build_triangles(self.ctx.handle, _addr(triangles), total,
                                                             _addr(offsets), n_meshes, self._h))
         self._keep = (triangles, offsets)
-        self.offsets = offsets if isinstance(offsets, np.ndarray) else offsets.cpu().numpy().view(np.uint32)
+        self._offsets = offsets  # read back lazily: build() stays free of host syncs
+        self._offsets_host = None
         return self
+
+    @property
+    def offsets(self) -> np.ndarray:
+        if self._offsets_host is None and self._offsets is not None:
+            o = self._offsets
+            self._offsets_host = o if isinstance(o, np.ndarray) else o.cpu().numpy().view(np.uint32)
+        return self._offsets_host
 
     def info(self):
         a, b, c = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
