@@ -182,6 +182,10 @@ LBVH_API int lbvh_bvh_curve(lbvh_ctx* ctx, const lbvh_bvh* bvh, uint32_t* codes,
  * 2055-2075) for m rays: rays is m x 8 float32, hits receives m lbvh_hit.
  * Requires a BVH built from triangles. */
 LBVH_API int lbvh_trace_triangles(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m, void* hits);
+/* Makes the BVH's traversal copy now, on the context's stream (traces make
+ * it on first use otherwise). Callers that trace one BVH from several streams
+ * call this once after each build / refit / import, before those traces. */
+LBVH_API int lbvh_bvh_prepare_trace(lbvh_ctx* ctx, lbvh_bvh* bvh);
 /* Same, also writing per-ray counts of box tests and triangle tests. */
 LBVH_API int lbvh_trace_triangles_counts(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m,
                                 void* hits, uint32_t* n_box, uint32_t* n_tri);
@@ -203,6 +207,8 @@ LBVH_API int lbvh_batch_destroy(lbvh_ctx* ctx, lbvh_batch* batch);
 LBVH_API int lbvh_batch_build_triangles(lbvh_ctx* ctx, const float* tris, size_t total, const uint32_t* offsets,
                                         size_t n_meshes, lbvh_batch* batch);
 LBVH_API int lbvh_batch_info(const lbvh_batch* batch, size_t* n_meshes, size_t* total_prims, size_t* total_nodes);
+/* As lbvh_bvh_prepare_trace, for a batch. */
+LBVH_API int lbvh_batch_prepare_trace(lbvh_ctx* ctx, lbvh_batch* batch);
 /* Copies all node blocks (total_prims - n_meshes nodes of 32 bytes). */
 LBVH_API int lbvh_batch_nodes(lbvh_ctx* ctx, const lbvh_batch* batch, void* dst);
 /* Traces rays [ray_offsets[k], ray_offsets[k + 1]) against mesh k (m rays in

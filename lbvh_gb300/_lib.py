@@ -60,6 +60,8 @@ SIGNATURES = {
     "lbvh_trace_triangles": (_I, [_P, _P, _P, _S, _P]),
     "lbvh_trace_triangles_counts": (_I, [_P, _P, _P, _S, _P, _P, _P]),
     "lbvh_build_triangles_noalloc": (_I, [_P, _S, _P, _P, _P]),
+    "lbvh_bvh_prepare_trace": (_I, [_P, _P]),
+    "lbvh_batch_prepare_trace": (_I, [_P, _P]),
     "lbvh_batch_create": (_I, [_P, _PP]),
     "lbvh_batch_destroy": (_I, [_P, _P]),
     "lbvh_batch_build_triangles": (_I, [_P, _P, _S, _P, _S, _P]),

@@ -735,6 +735,33 @@ lbvh_bvh_curve(lbvh_ctx* c, const lbvh_bvh* b, uint32_t* codes, uint32_t* sorted
   return host ? check_device(c) : LBVH_OK;
 }
 
+// The traversal copy of a BVH is a cache, made on first use after a build,
+// refit or import.
+static int
+ensure_wnodes(lbvh_ctx* c, lbvh_bvh* b)
+{
+  if (b->wnodes_valid)
+    return LBVH_OK;
+  CK(reserve(b->wnodes, sizeof(WideNode) * b->n, c->stream), "traversal layout allocation");
+  CK(launch_repack(static_cast<const Node*>(b->nodes.ptr), b->n - 1, static_cast<WideNode*>(b->wnodes.ptr), c->stream),
+     "repack launch");
+  b->wnodes_valid = true;
+  return LBVH_OK;
+}
+
+int
+lbvh_bvh_prepare_trace(lbvh_ctx* c, lbvh_bvh* b)
+{
+  if (!c || !b)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (b->n < 2 || b->kind != kKindTris)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH was not built from triangles");
+  int st = set_device(c);
+  if (st)
+    return st;
+  return ensure_wnodes(c, b);
+}
+
 static int
 trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* hits, uint32_t* n_box, uint32_t* n_tri)
 {
@@ -778,14 +805,8 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
                                                           : static_cast<const Tri*>(b->prims);
   const uint32_t* leaf_prim =
     (b->flags & LBVH_BUILD_SORTED_LEAVES) ? static_cast<const uint32_t*>(b->leaf_prim.ptr) : nullptr;
-  lbvh_bvh* mb = const_cast<lbvh_bvh*>(b); // the traversal copy is a cache
-  if (!mb->wnodes_valid) {
-    CK(reserve(mb->wnodes, sizeof(WideNode) * b->n, c->stream), "traversal layout allocation");
-    CK(launch_repack(static_cast<const Node*>(b->nodes.ptr), b->n - 1, static_cast<WideNode*>(mb->wnodes.ptr),
-                     c->stream),
-       "repack launch");
-    mb->wnodes_valid = true;
-  }
+  if ((st = ensure_wnodes(c, const_cast<lbvh_bvh*>(b))))
+    return st;
   CK(launch_trace_tris(static_cast<const WideNode*>(b->wnodes.ptr), b->n - 1, tris, leaf_prim, dr, uint32_t(m), dh,
                        counts ? db : nullptr, counts ? dt : nullptr, c->ray_counter, c->num_sms, c->trace,
                        c->stream),
@@ -853,9 +874,36 @@ host_offsets_ok(lbvh_ctx* c, const uint32_t* off, size_t n_meshes, size_t total,
   return LBVH_OK;
 }
 
+int
+batch_wnodes(lbvh_ctx* c, lbvh_batch* b)
+{
+  if (b->wnodes_valid)
+    return LBVH_OK;
+  const uint32_t total_nodes = b->total - b->n_meshes;
+  CK(reserve(b->wnodes, sizeof(WideNode) * (total_nodes + 1), c->stream), "traversal layout allocation");
+  CK(launch_batch_repack(static_cast<const Node*>(b->nodes.ptr), total_nodes, static_cast<const uint32_t*>(b->off.ptr),
+                         b->n_meshes, static_cast<WideNode*>(b->wnodes.ptr), c->stream),
+     "repack launch");
+  b->wnodes_valid = true;
+  return LBVH_OK;
+}
+
 } // namespace
 
 extern "C" {
+
+int
+lbvh_batch_prepare_trace(lbvh_ctx* c, lbvh_batch* b)
+{
+  if (!c || !b)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (!b->n_meshes)
+    return fail(c, LBVH_ERR_INVALID_ARG, "batch has not been built");
+  int st = set_device(c);
+  if (st)
+    return st;
+  return batch_wnodes(c, b);
+}
 
 int
 lbvh_batch_create(lbvh_ctx* c, lbvh_batch** out)
@@ -987,13 +1035,8 @@ lbvh_batch_trace_triangles(lbvh_ctx* c, const lbvh_batch* b, const float* rays, 
     return LBVH_OK;
   lbvh_batch* mb = const_cast<lbvh_batch*>(b); // traversal copy and offsets are caches
   const uint32_t total_nodes = b->total - b->n_meshes;
-  if (!mb->wnodes_valid) {
-    CK(reserve(mb->wnodes, sizeof(WideNode) * (total_nodes + 1), c->stream), "traversal layout allocation");
-    CK(launch_batch_repack(static_cast<const Node*>(b->nodes.ptr), total_nodes, static_cast<const uint32_t*>(b->off.ptr),
-                           b->n_meshes, static_cast<WideNode*>(mb->wnodes.ptr), c->stream),
-       "repack launch");
-    mb->wnodes_valid = true;
-  }
+  if ((st = batch_wnodes(c, mb)))
+    return st;
   CK(reserve(mb->roff, 4 * (b->n_meshes + 1), c->stream), "ray offset allocation");
   CK(cudaMemcpyAsync(mb->roff.ptr, ray_offsets, 4 * (b->n_meshes + 1), cudaMemcpyDefault, c->stream),
      "ray offset upload");

@@ -369,3 +369,71 @@ def batch_scene(k: int = 4096, lo: int = 64, hi: int = 65536, rays_per_mesh: int
     rays = random_rays_in_box([-1.0] * 3, [1.0] * 3, k * rays_per_mesh, seed, stream=80)
     ray_offsets = (np.arange(k + 1, dtype=np.int64) * rays_per_mesh).astype(np.uint32)
     return tris, offsets, rays, ray_offsets
+
+
+def torus_mesh(n_target: int, seed: int, major: float = 1.0, minor: float = 0.35) -> np.ndarray:
+    """A torus tessellated to about n_target triangles in (u, v) grid order
+    (coherent input order, so the reference's leaf order gives a usable tree),
+    placed at a seeded offset."""
+    quads = max(1, n_target // 2)
+    nv = max(3, int(round(math.sqrt(quads / 2.0))))
+    nu = max(3, quads // nv)
+    iu, iv = np.meshgrid(np.arange(nu), np.arange(nv), indexing="ij")
+    iu = iu.reshape(-1)
+    iv = iv.reshape(-1)
+    shift = (uniform(seed, 90, 3) * 2.0 - 1.0) * 2.0
+
+    def p(u, v):
+        a = 2.0 * math.pi * u / nu
+        b = 2.0 * math.pi * v / nv
+        r = major + minor * np.cos(b)
+        return np.stack([r * np.cos(a), r * np.sin(a), minor * np.sin(b)], -1) + shift
+
+    p00, p10 = p(iu, iv), p(iu + 1, iv)
+    p01, p11 = p(iu, iv + 1), p(iu + 1, iv + 1)
+    t = np.stack([np.stack([p00, p10, p11], 1), np.stack([p00, p11, p01], 1)], 1).reshape(-1, 3, 3)
+    return make_triangles(t.astype(np.float32))
+
+
+def jitter(tris: np.ndarray, seed: int, sigma: float = 0.01) -> np.ndarray:
+    """Seeded vertex jitter N(0, sigma) of every triangle's vertices (the
+    served workload's refit input)."""
+    v = triangle_vertices(tris).reshape(-1, 9).astype(np.float64)
+    v += normal(seed, 95, v.size).reshape(v.shape) * sigma
+    return make_triangles(v.astype(np.float32))
+
+
+def served_requests(n_requests: int, rate: float, seed: int, n_scenes: int = 48, lo: int = 1000, hi: int = 2_000_000,
+                    ray_lo: int = 16384, ray_hi: int = 2_000_000, ray_pool: int = 4):
+    """Served workload: Poisson arrivals at `rate` requests/s. First one build
+    per scene (sizes log-uniform in [lo, hi] triangles, torus meshes), then a
+    seeded mix of 70% traces (log-uniform [ray_lo, ray_hi] rays, a slice of a
+    pooled incoherent ray set), 20% refits (vertex jitter N(0, 0.01)) and 10%
+    rebuilds, each on a uniformly chosen scene.
+    Returns [(arrival_s, kind, scene, data)] in arrival order."""
+    sizes = log_uniform_counts(n_scenes, lo, hi, seed)
+    meshes = [torus_mesh(int(sizes[s]), seed * 7919 + s) for s in range(n_scenes)]
+    pool = [incoherent_rays(meshes[k % n_scenes], ray_hi, seed + 100 + k, scale=1.2) for k in range(ray_pool)]
+    gaps = -np.log1p(-uniform(seed, 96, n_requests)) / rate
+    t = np.cumsum(gaps)
+    kinds = uniform(seed, 97, n_requests)
+    who = np.minimum((uniform(seed, 98, n_requests) * n_scenes).astype(np.int64), n_scenes - 1)
+    nr = log_uniform_counts(n_requests, ray_lo, ray_hi, seed + 1)
+    cur = list(meshes)
+    out = []
+    for i in range(n_requests):
+        if i < n_scenes:
+            out.append((float(t[i]), "build", i, cur[i]))
+            continue
+        s = int(who[i])
+        if kinds[i] < 0.7:
+            rays = pool[i % ray_pool]
+            start = int(uniform(seed, 99, 1, i)[0] * (rays.shape[0] - nr[i]))
+            out.append((float(t[i]), "trace", s, rays[start : start + int(nr[i])]))
+        elif kinds[i] < 0.9:
+            cur[s] = jitter(cur[s], seed * 31 + i)
+            out.append((float(t[i]), "refit", s, cur[s]))
+        else:
+            cur[s] = torus_mesh(int(sizes[s]), seed * 7919 + s + 1_000_000 * (i + 1))[: cur[s].shape[0]]
+            out.append((float(t[i]), "build", s, cur[s]))
+    return out

@@ -1,0 +1,65 @@
+"""The request server: every result of a mixed, overlapping request stream
+equals the same request run alone through the plain API (bit for bit), with
+coalesced small builds/traces, several streams, and LRU eviction under a
+small HBM budget."""
+import numpy as np
+import pytest
+
+import lbvh_gb300 as lb
+from lbvh_gb300 import scenes
+from lbvh_gb300.serve import Server, run_plain, scene_bytes
+from conftest import hit_mismatches
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _stream(n=160, n_scenes=20, hi=150_000, seed=4):
+    return scenes.served_requests(n, 2000.0, seed, n_scenes=n_scenes, lo=300, hi=hi, ray_lo=1000,
+                                  ray_hi=120_000)
+
+
+def _serve(reqs, **kw):
+    with Server(**kw) as srv:
+        futs = [srv.submit(kind, scene, data) for _, kind, scene, data in reqs]
+        results = [f.result(timeout=120) for f in futs]
+        stats = {"coalesced": srv.coalesced, "evictions": srv.evictions}
+    return results, stats
+
+
+def test_mixed_stream_matches_plain_path(lib_built):
+    assert torch.cuda.is_available()
+    reqs = _stream()
+    plain = run_plain([(0.0, k, s, d) for _, k, s, d in reqs])
+    got, stats = _serve(reqs, slots=4)
+    assert stats["coalesced"] > 0  # the initial small builds were batched
+    for (_, kind, scene, _), (want, _), res in zip(reqs, plain, got):
+        if kind == "trace":
+            assert hit_mismatches(res, want).size == 0, scene
+        else:
+            assert res is None
+
+
+def test_eviction_under_a_small_budget(lib_built):
+    # room for a few scenes only: scenes without queued work are evicted, the
+    # results stay the same
+    reqs = _stream(n=80, n_scenes=12, hi=60_000, seed=5)
+    plain = run_plain([(0.0, k, s, d) for _, k, s, d in reqs])
+    budget = 4 * scene_bytes(60_000)
+    got, stats = _serve(reqs, slots=3, hbm_budget=budget, batch_max_tris=0)
+    assert stats["evictions"] > 0
+    for (_, kind, _, _), (want, _), res in zip(reqs, plain, got):
+        if kind == "trace":
+            assert hit_mismatches(res, want).size == 0
+
+
+def test_trace_of_unknown_scene_fails_cleanly(lib_built):
+    with Server(slots=1) as srv:
+        f = srv.submit("trace", 12345, scenes.pinhole_rays(4, 4))
+        with pytest.raises(KeyError):
+            f.result(timeout=30)
+        t = scenes.soup(100, 1)
+        srv.submit("build", 1, t).result(timeout=30)
+        hits = srv.submit("trace", 1, scenes.incoherent_rays(t, 500, 2)).result(timeout=30)
+        assert hits.shape == (500,)
