@@ -408,22 +408,25 @@ def served_requests(n_requests: int, rate: float, seed: int, n_scenes: int = 48,
     """Served workload: Poisson arrivals at `rate` requests/s. First one build
     per scene (sizes log-uniform in [lo, hi] triangles, torus meshes), then a
     seeded mix of 70% traces (log-uniform [ray_lo, ray_hi] rays, a slice of a
-    pooled incoherent ray set), 20% refits (vertex jitter N(0, 0.01)) and 10%
-    rebuilds, each on a uniformly chosen scene.
-    Returns [(arrival_s, kind, scene, data)] in arrival order."""
+    pooled incoherent ray set), 20% refits (vertex jitter N(0, 0.01); each
+    scene alternates between two jittered variants of its mesh) and 10% full
+    rebuilds (of the scene's unjittered mesh), each on a uniformly chosen
+    scene. Returns [(arrival_s, kind, scene, data)] in arrival order; data
+    arrays are shared between requests."""
     sizes = log_uniform_counts(n_scenes, lo, hi, seed)
     meshes = [torus_mesh(int(sizes[s]), seed * 7919 + s) for s in range(n_scenes)]
+    variants = [(jitter(m, seed * 31 + 2 * s), jitter(m, seed * 31 + 2 * s + 1)) for s, m in enumerate(meshes)]
     pool = [incoherent_rays(meshes[k % n_scenes], ray_hi, seed + 100 + k, scale=1.2) for k in range(ray_pool)]
     gaps = -np.log1p(-uniform(seed, 96, n_requests)) / rate
     t = np.cumsum(gaps)
     kinds = uniform(seed, 97, n_requests)
     who = np.minimum((uniform(seed, 98, n_requests) * n_scenes).astype(np.int64), n_scenes - 1)
     nr = log_uniform_counts(n_requests, ray_lo, ray_hi, seed + 1)
-    cur = list(meshes)
+    flip = [0] * n_scenes
     out = []
     for i in range(n_requests):
         if i < n_scenes:
-            out.append((float(t[i]), "build", i, cur[i]))
+            out.append((float(t[i]), "build", i, meshes[i]))
             continue
         s = int(who[i])
         if kinds[i] < 0.7:
@@ -431,9 +434,8 @@ def served_requests(n_requests: int, rate: float, seed: int, n_scenes: int = 48,
             start = int(uniform(seed, 99, 1, i)[0] * (rays.shape[0] - nr[i]))
             out.append((float(t[i]), "trace", s, rays[start : start + int(nr[i])]))
         elif kinds[i] < 0.9:
-            cur[s] = jitter(cur[s], seed * 31 + i)
-            out.append((float(t[i]), "refit", s, cur[s]))
+            out.append((float(t[i]), "refit", s, variants[s][flip[s]]))
+            flip[s] ^= 1
         else:
-            cur[s] = torus_mesh(int(sizes[s]), seed * 7919 + s + 1_000_000 * (i + 1))[: cur[s].shape[0]]
-            out.append((float(t[i]), "build", s, cur[s]))
+            out.append((float(t[i]), "build", s, meshes[s]))
     return out

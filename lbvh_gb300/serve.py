@@ -36,7 +36,7 @@ from . import api as lbapi
 BUILD, REFIT, TRACE = "build", "refit", "trace"
 
 
-@dataclass
+@dataclass(eq=False)  # requests are compared by identity
 class Request:
     kind: str
     scene: int
@@ -47,7 +47,7 @@ class Request:
     done: float = 0.0
 
 
-@dataclass
+@dataclass(eq=False)
 class Resident:
     """A scene on the device: its own BVH, or member `index` of a batch."""
     n: int
@@ -61,7 +61,7 @@ class Resident:
     retired: bool = False       # replaced or evicted, freed when busy drops to 0
 
 
-@dataclass
+@dataclass(eq=False)
 class _BatchRef:
     batch: object               # lbapi.Batch
     tris: object                # device triangles of all members
@@ -285,8 +285,16 @@ class Server:
             res = self.resident[chosen.scene]
             group = [chosen]
             if res.batch is not None and chosen.data.shape[0] <= self.trace_batch_max_rays:
+                # a trace may run ahead of other traces, never ahead of an
+                # earlier build or refit of its scene
+                stopped = set(blocked)
                 for r in queue:
-                    if r is chosen or r.kind != TRACE or r.scene in blocked:
+                    if r is chosen:
+                        continue
+                    if r.kind != TRACE:
+                        stopped.add(r.scene)
+                        continue
+                    if r.scene in stopped:
                         continue
                     other = self.resident.get(r.scene)
                     if other is not None and other.batch is res.batch and r.scene not in self.writing \

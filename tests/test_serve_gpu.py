@@ -42,16 +42,21 @@ def test_mixed_stream_matches_plain_path(lib_built):
 
 
 def test_eviction_under_a_small_budget(lib_built):
-    # room for a few scenes only: scenes without queued work are evicted, the
-    # results stay the same
-    reqs = _stream(n=80, n_scenes=12, hi=60_000, seed=5)
-    plain = run_plain([(0.0, k, s, d) for _, k, s, d in reqs])
-    budget = 4 * scene_bytes(60_000)
-    got, stats = _serve(reqs, slots=3, hbm_budget=budget, batch_max_tris=0)
-    assert stats["evictions"] > 0
-    for (_, kind, _, _), (want, _), res in zip(reqs, plain, got):
-        if kind == "trace":
-            assert hit_mismatches(res, want).size == 0
+    # room for four scenes: each new build evicts the least recently used
+    # scene without queued work; the scenes still resident trace correctly
+    meshes = [scenes.torus_mesh(40_000, 50 + k) for k in range(10)]
+    budget = 4 * scene_bytes(meshes[0].shape[0]) + 1024
+    with Server(slots=2, hbm_budget=budget, batch_max_tris=0) as srv:
+        for k, m in enumerate(meshes):
+            srv.submit("build", k, m).result(timeout=60)
+        assert srv.evictions >= 6
+        assert sorted(srv.resident) == [6, 7, 8, 9]
+        rays = scenes.incoherent_rays(meshes[9], 20_000, 1)
+        got = srv.submit("trace", 9, rays).result(timeout=60)
+        with pytest.raises(KeyError):
+            srv.submit("trace", 0, rays).result(timeout=60)  # evicted
+    want = run_plain([(0.0, "build", 9, meshes[9]), (0.0, "trace", 9, rays)])[1][0]
+    assert hit_mismatches(got, want).size == 0
 
 
 def test_trace_of_unknown_scene_fails_cleanly(lib_built):
