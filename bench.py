@@ -201,6 +201,61 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
                          "traffic": None, "peak_kind": peak_kind}}
 
 
+def _pct(xs, q):
+    return round(1e3 * float(np.percentile(np.asarray(xs), q)), 3) if len(xs) else None
+
+
+def measure_served(device, n_requests=400, rate=2000.0, seed=7):
+    """Served workload: Poisson arrivals of build / refit / trace requests on
+    48 resident scenes (1k-2M triangles, 16k-2M rays per trace) through the
+    request server (4 streams, coalescing, 120 GB HBM budget), against the same
+    arrivals through the plain API one request at a time. Latency is measured
+    from each request's arrival."""
+    import torch
+
+    from lbvh_gb300 import scenes
+    from lbvh_gb300.serve import Server, run_plain
+
+    reqs = scenes.served_requests(n_requests, rate, seed, n_scenes=48)
+    kinds = [k for _, k, _, _ in reqs]
+    with Server(device, slots=4, hbm_budget=120 << 30) as srv:
+        srv.submit("build", -1, scenes.soup(1000, 1)).result()  # library warm-up
+        srv.submit("trace", -1, scenes.pinhole_rays(64, 64)).result()
+        srv.done.clear()
+        futs = []
+        t0 = time.perf_counter()
+        for at, kind, scene, data in reqs:
+            wait = t0 + at - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            futs.append(srv.submit(kind, scene, data))
+        results = [f.result(timeout=600) for f in futs]
+        done = list(srv.done)
+        coalesced, evictions = srv.coalesced, srv.evictions
+    lat = [r.done - r.arrival for r in done]
+    span = max(r.done for r in done) - min(r.arrival for r in done)
+    by_kind = {}
+    for r in done:
+        by_kind.setdefault(r.kind, []).append(r.done - r.arrival)
+    plain = run_plain(reqs, device)
+    plat = [x[1] for x in plain]
+    pspan = max(at + l for (at, _, _, _), l in zip(reqs, plat)) - reqs[0][0]
+    same = all(a is None and b is None or (a is not None and b is not None and a.tobytes() == b.tobytes())
+               for a, (b, _) in zip(results, plain))
+    rays = sum(d.shape[0] for _, k, _, d in reqs if k == "trace")
+    del results, plain
+    torch.cuda.empty_cache()
+    return {"requests": n_requests, "rate_per_s": rate, "scenes": 48,
+            "mix": {k: kinds.count(k) for k in ("build", "refit", "trace")},
+            "server": {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "throughput_req_s": round(len(lat) / span, 1),
+                       "trace_mrays_s": round(rays / span / 1e6, 1), "coalesced_requests": coalesced,
+                       "evictions": evictions,
+                       "by_kind": {k: {"p50_ms": _pct(v, 50), "p99_ms": _pct(v, 99)} for k, v in by_kind.items()}},
+            "plain": {"p50_ms": _pct(plat, 50), "p99_ms": _pct(plat, 99),
+                      "throughput_req_s": round(len(plat) / pspan, 1), "trace_mrays_s": round(rays / pspan / 1e6, 1)},
+            "results_equal": bool(same)}
+
+
 def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_per_mesh=4096, seed=3):
     """Batched workload: n_meshes soups with log-uniform [64, 65,536]
     triangles and rays_per_mesh random rays each. Build + trace of all meshes
@@ -316,6 +371,8 @@ def main():
     ap.add_argument("--soup-n", type=int, default=N_BUILD_16M, help="soup size of the build measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
     ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-requests measurement")
+    ap.add_argument("--only-served", action="store_true", help="only the served-requests measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -338,6 +395,12 @@ def main():
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     ctx = lb.Context(local, stream.cuda_stream)
+
+    if args.only_served:
+        r = measure_served(local)
+        if rank == 0:
+            print(json.dumps({"served": r}), flush=True)
+        return 0
 
     if args.only_batched:
         r = measure_batched(local, args.steps, hbm_peak, peak_kind)
@@ -456,6 +519,11 @@ def main():
     if not args.no_batched:
         batched = measure_batched(local, args.steps, hbm_peak, peak_kind)
 
+    # ---- served requests vs the plain path ---------------------------------
+    served = None
+    if not args.no_served:
+        served = measure_served(local)
+
     # ---- CPU baseline: the oracle port (or reference) on the host cores ---
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -491,6 +559,7 @@ def main():
                   "hit_fraction": round(hit_frac, 4)},
         "build_16m": build_16m,
         "batched": batched,
+        "served": served,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
