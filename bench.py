@@ -205,19 +205,14 @@ def _pct(xs, q):
     return round(1e3 * float(np.percentile(np.asarray(xs), q)), 3) if len(xs) else None
 
 
-def measure_served(device, n_requests=400, rate=2000.0, seed=7):
-    """Served workload: Poisson arrivals of build / refit / trace requests on
-    48 resident scenes (1k-2M triangles, 16k-2M rays per trace) through the
-    request server (4 streams, coalescing, 120 GB HBM budget), against the same
-    arrivals through the plain API one request at a time. Latency is measured
-    from each request's arrival."""
+def _served_run(reqs, device):
+    """One arrival stream through the request server and through the plain
+    API; latency from each request's arrival."""
     import torch
 
     from lbvh_gb300 import scenes
     from lbvh_gb300.serve import Server, run_plain
 
-    reqs = scenes.served_requests(n_requests, rate, seed, n_scenes=48)
-    kinds = [k for _, k, _, _ in reqs]
     with Server(device, slots=4, hbm_budget=120 << 30) as srv:
         srv.submit("build", -1, scenes.soup(1000, 1)).result()  # library warm-up
         srv.submit("trace", -1, scenes.pinhole_rays(64, 64)).result()
@@ -240,20 +235,45 @@ def measure_served(device, n_requests=400, rate=2000.0, seed=7):
     plain = run_plain(reqs, device)
     plat = [x[1] for x in plain]
     pspan = max(at + l for (at, _, _, _), l in zip(reqs, plat)) - reqs[0][0]
-    same = all(a is None and b is None or (a is not None and b is not None and a.tobytes() == b.tobytes())
-               for a, (b, _) in zip(results, plain))
+    bad = [i for i, (a, (b, _)) in enumerate(zip(results, plain))
+           if not (a is None and b is None or (a is not None and b is not None and a.tobytes() == b.tobytes()))]
     rays = sum(d.shape[0] for _, k, _, d in reqs if k == "trace")
     del results, plain
     torch.cuda.empty_cache()
-    return {"requests": n_requests, "rate_per_s": rate, "scenes": 48,
-            "mix": {k: kinds.count(k) for k in ("build", "refit", "trace")},
-            "server": {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "throughput_req_s": round(len(lat) / span, 1),
-                       "trace_mrays_s": round(rays / span / 1e6, 1), "coalesced_requests": coalesced,
-                       "evictions": evictions,
-                       "by_kind": {k: {"p50_ms": _pct(v, 50), "p99_ms": _pct(v, 99)} for k, v in by_kind.items()}},
-            "plain": {"p50_ms": _pct(plat, 50), "p99_ms": _pct(plat, 99),
-                      "throughput_req_s": round(len(plat) / pspan, 1), "trace_mrays_s": round(rays / pspan / 1e6, 1)},
-            "results_equal": bool(same)}
+    kinds = [k for _, k, _, _ in reqs]
+    out = {"requests": len(reqs), "mix": {k: kinds.count(k) for k in ("build", "refit", "trace")},
+           "server": {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "throughput_req_s": round(len(lat) / span, 1),
+                      "trace_mrays_s": round(rays / span / 1e6, 1), "coalesced_requests": coalesced,
+                      "evictions": evictions,
+                      "by_kind": {k: {"p50_ms": _pct(v, 50), "p99_ms": _pct(v, 99)} for k, v in by_kind.items()}},
+           "plain": {"p50_ms": _pct(plat, 50), "p99_ms": _pct(plat, 99),
+                     "throughput_req_s": round(len(plat) / pspan, 1), "trace_mrays_s": round(rays / pspan / 1e6, 1)},
+           "results_equal": not bad}
+    out["throughput_ratio"] = round(out["server"]["throughput_req_s"] / out["plain"]["throughput_req_s"], 2)
+    if bad:
+        out["mismatched"] = [[i, reqs[i][1], reqs[i][2]] for i in bad[:8]]
+    return out
+
+
+def measure_served(device, seed=7):
+    """Served workloads (Poisson arrivals of build / refit / trace requests on
+    48 resident scenes, 70% trace / 20% refit / 10% rebuild after one build
+    per scene) through the request server (4 streams, coalescing, 120 GB HBM
+    budget), against the same arrivals through the plain API one request at a
+    time:
+      mix:   scenes 1k-2M triangles, traces 16k-2M rays, 400 requests at
+             2,000 requests/s;
+      small: scenes 1k-64k triangles, traces 16k-64k rays, 2,000 requests at
+             20,000 requests/s (both paths saturated)."""
+    from lbvh_gb300 import scenes
+
+    mix = scenes.served_requests(400, 2000.0, seed, n_scenes=48)
+    out = {"mix": dict(rate_per_s=2000.0, scenes=48, **_served_run(mix, device))}
+    del mix
+    small = scenes.served_requests(2000, 20000.0, seed + 1, n_scenes=48, lo=1000, hi=65536, ray_lo=16384,
+                                   ray_hi=65536)
+    out["small"] = dict(rate_per_s=20000.0, scenes=48, **_served_run(small, device))
+    return out
 
 
 def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_per_mesh=4096, seed=3):

@@ -212,7 +212,9 @@ LBVH_API int lbvh_batch_prepare_trace(lbvh_ctx* ctx, lbvh_batch* batch);
 /* Copies all node blocks (total_prims - n_meshes nodes of 32 bytes). */
 LBVH_API int lbvh_batch_nodes(lbvh_ctx* ctx, const lbvh_batch* batch, void* dst);
 /* Traces rays [ray_offsets[k], ray_offsets[k + 1]) against mesh k (m rays in
- * all, n_meshes + 1 offsets); hit primitive ids are mesh-local. */
+ * all, n_meshes + 1 offsets); hit primitive ids are mesh-local. Host ray
+ * offsets are staged in the context, so once lbvh_batch_prepare_trace has
+ * run, contexts on different streams may trace one batch at the same time. */
 LBVH_API int lbvh_batch_trace_triangles(lbvh_ctx* ctx, const lbvh_batch* batch, const float* rays,
                                         const uint32_t* ray_offsets, size_t m, void* hits);
 

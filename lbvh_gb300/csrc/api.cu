@@ -46,6 +46,7 @@ struct lbvh_ctx
   DevBuf hits;                 // staging for host hits
   DevBuf counts;               // staging for host per-ray counts
   DevBuf prims_in;             // staging for host refit input
+  DevBuf roff;                 // staging for host batch ray offsets
   uint32_t* ray_counter = nullptr; // persistent-trace ray dispenser
   TraceParams trace;               // traversal launch shape
   uint32_t batch_threads = 512;    // CTA size of the batched build
@@ -482,6 +483,7 @@ lbvh_ctx_destroy(lbvh_ctx* c)
   release(c->hits, c->stream);
   release(c->counts, c->stream);
   release(c->prims_in, c->stream);
+  release(c->roff, c->stream);
   cudaStreamSynchronize(c->stream);
   cudaFree(c->state);
   cudaFree(c->ray_counter);
@@ -853,7 +855,6 @@ struct lbvh_batch
   DevBuf nodes;              // total - n_meshes nodes
   DevBuf wnodes;             // traversal copy + flag word
   bool wnodes_valid = false;
-  DevBuf roff;               // device copy of the ray offsets
 };
 
 namespace {
@@ -927,7 +928,6 @@ lbvh_batch_destroy(lbvh_ctx* c, lbvh_batch* b)
   release(b->tris_owned, c->stream);
   release(b->nodes, c->stream);
   release(b->wnodes, c->stream);
-  release(b->roff, c->stream);
   delete b;
   return LBVH_OK;
 }
@@ -1033,13 +1033,21 @@ lbvh_batch_trace_triangles(lbvh_ctx* c, const lbvh_batch* b, const float* rays, 
     return st;
   if (m == 0)
     return LBVH_OK;
-  lbvh_batch* mb = const_cast<lbvh_batch*>(b); // traversal copy and offsets are caches
+  lbvh_batch* mb = const_cast<lbvh_batch*>(b); // the traversal copy is a cache
   const uint32_t total_nodes = b->total - b->n_meshes;
   if ((st = batch_wnodes(c, mb)))
     return st;
-  CK(reserve(mb->roff, 4 * (b->n_meshes + 1), c->stream), "ray offset allocation");
-  CK(cudaMemcpyAsync(mb->roff.ptr, ray_offsets, 4 * (b->n_meshes + 1), cudaMemcpyDefault, c->stream),
-     "ray offset upload");
+  // Host ray offsets are staged in the context, never in the batch, so that
+  // contexts on different streams can trace one batch at the same time.
+  const uint32_t* droff = ray_offsets;
+  if (!on_device(ray_offsets)) {
+    CK(reserve(c->roff, 4 * (b->n_meshes + 1), c->stream), "ray offset allocation");
+    CK(cudaMemcpyAsync(c->roff.ptr, ray_offsets, 4 * (b->n_meshes + 1), cudaMemcpyHostToDevice, c->stream),
+       "ray offset upload");
+    droff = static_cast<const uint32_t*>(c->roff.ptr);
+  } else if (reinterpret_cast<uintptr_t>(ray_offsets) & 3) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device ray offsets must be 4-byte aligned");
+  }
   const bool hr = !on_device(rays), hh = !on_device(hits);
   const float* dr = rays;
   Hit* dh = static_cast<Hit*>(hits);
@@ -1057,7 +1065,7 @@ lbvh_batch_trace_triangles(lbvh_ctx* c, const lbvh_batch* b, const float* rays, 
     return fail(c, LBVH_ERR_INVALID_ARG, "device hits must be 16-byte aligned");
   }
   CK(launch_batch_trace(static_cast<const WideNode*>(mb->wnodes.ptr), total_nodes, static_cast<const Tri*>(b->tris),
-                        static_cast<const uint32_t*>(b->off.ptr), static_cast<const uint32_t*>(mb->roff.ptr),
+                        static_cast<const uint32_t*>(b->off.ptr), droff,
                         b->n_meshes, dr, uint32_t(m), dh, c->ray_counter, c->num_sms, c->trace, c->stream),
      "batch trace launch");
   if (hh)

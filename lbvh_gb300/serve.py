@@ -1,9 +1,10 @@
 """Request server: build / refit / trace requests on device-resident BVHs.
 
-Requests arrive over time (submit() from any thread) and are served by one
-dispatch thread over `slots` CUDA streams, each with its own lbvh context, so
-work admitted while other work is on the GPU runs concurrently with it
-(continuous batching, not a queue drained one request at a time):
+Requests arrive over time (submit() from any thread). One dispatch thread
+decides what runs; `slots` worker threads, each with its own CUDA stream and
+lbvh context, run it, so work admitted while other work is on the GPU runs
+concurrently with it (continuous batching, not a queue drained one request
+at a time):
 
 * every scene's BVH stays resident on the device between requests;
 * admission is against an HBM budget: a request that needs memory evicts
@@ -15,15 +16,25 @@ work admitted while other work is on the GPU runs concurrently with it
 * requests on one scene keep their submission order (a trace submitted after
   a refit sees the refitted tree); requests on different scenes overlap.
 
+Host data moves straight between the caller's (pageable) arrays and the
+device, each request's copy issued by the worker that runs it: on a
+Grace-Blackwell node the copy engines read and write pageable memory through
+the shared address space at full link speed, while a CPU copy into a pinned
+staging buffer runs at single-core memcpy speed, so no staging buffers are
+used. Result arrays are touched (one byte per page) while the kernel runs,
+so the device-to-host copy lands in mapped pages.
+
 Every result equals running the same request alone through the plain API
 (Builder / BVH.refit / Traverser): the kernels are the same and the
 arithmetic is bit-identical to the reference.
 
-Latency = completion seen by the dispatcher - arrival (submit) time.
+Latency = completion of the request's GPU work and result copy, as seen by
+its worker, minus arrival (submit) time.
 """
 from __future__ import annotations
 
 import collections
+import queue
 import threading
 import time
 from concurrent.futures import Future
@@ -31,6 +42,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _lib
 from . import api as lbapi
 
 BUILD, REFIT, TRACE = "build", "refit", "trace"
@@ -75,19 +87,65 @@ def scene_bytes(n: int) -> int:
     return 144 * n + (1 << 16)
 
 
+def _touch(a: np.ndarray) -> None:
+    """Maps a fresh array's pages (one write per 4 KiB)."""
+    b = a.reshape(-1).view(np.uint8)
+    b[::4096] = 0
+
+
+class _Job:
+    __slots__ = ("work", "finish", "fail", "out", "err", "t_done")
+
+    def __init__(self, work, finish, fail):
+        self.work, self.finish, self.fail = work, finish, fail
+        self.out = self.err = None
+        self.t_done = 0.0
+
+
 class _Slot:
-    def __init__(self, torch, device: int):
+    """A worker thread with its own stream and lbvh context. It runs one job
+    at a time: the job's work() issues copies and launches on the stream,
+    then the worker waits for the stream (and reads the context's device
+    error word) before reporting the job complete to the dispatcher."""
+
+    def __init__(self, server, torch, device: int, k: int):
+        self.server = server
+        self.torch = torch
+        self.device = device
         self.stream = torch.cuda.Stream(device)
         self.ctx = lbapi.Context(device, self.stream.cuda_stream)
         self.busy = False
-        self.pinned = {}
+        self.jobs: queue.SimpleQueue = queue.SimpleQueue()
+        self.thread = threading.Thread(target=self._run, name=f"lbvh-server-slot{k}", daemon=True)
+        self.thread.start()
 
-    def pinned_buffer(self, torch, key: str, nbytes: int):
-        buf = self.pinned.get(key)
-        if buf is None or buf.numel() < nbytes:
-            buf = torch.empty(max(nbytes, 1 << 20), dtype=torch.uint8).pin_memory()
-            self.pinned[key] = buf
-        return buf[:nbytes]
+    def _run(self):
+        torch = self.torch
+        torch.cuda.set_device(self.device)
+        while True:
+            job = self.jobs.get()
+            if job is None:
+                return
+            try:
+                with torch.cuda.stream(self.stream):
+                    job.out = job.work()
+                self.ctx.synchronize()
+            except BaseException as exc:  # reported to the job's requests
+                job.err = exc
+                try:
+                    self.stream.synchronize()
+                except BaseException:
+                    pass
+            job.t_done = time.perf_counter()
+            self.server._completed(self, job)
+
+    def upload(self, host: np.ndarray, width: int):
+        """Host rows -> new device float32 tensor [rows, width] (allocated on
+        this stream, copied straight from the host array)."""
+        torch = self.torch
+        dev = torch.empty((host.shape[0], width), dtype=torch.float32, device=self.device)
+        dev.copy_(torch.from_numpy(host), non_blocking=True)
+        return dev
 
 
 class Server:
@@ -101,7 +159,6 @@ class Server:
 
         self.torch = torch
         self.device = device
-        self.slots = [_Slot(torch, device) for _ in range(slots)]
         self.budget = int(hbm_budget)
         self.used = 0
         self.batch_max_tris = batch_max_tris
@@ -110,13 +167,15 @@ class Server:
         self.resident: "collections.OrderedDict[int, Resident]" = collections.OrderedDict()
         self.writing: set[int] = set()        # scenes with a running build / refit
         self.pending: collections.deque[Request] = collections.deque()
-        self.running: list = []               # (event, slot, finish callback)
         self.done: list[Request] = []
         self.evictions = 0
         self.coalesced = 0
         self._cv = threading.Condition()
+        self._dirty = False                   # a submit or a completion since the last scan
+        self._finished: list = []             # (slot, job) reported by workers
         self._stop = False
         self._error = None
+        self.slots = [_Slot(self, torch, device, k) for k in range(slots)]
         self._thread = threading.Thread(target=self._loop, name="lbvh-server", daemon=True)
         self._thread.start()
 
@@ -131,15 +190,19 @@ class Server:
             if self._stop:
                 raise RuntimeError("server is closed")
             self.pending.append(r)
+            self._dirty = True
             self._cv.notify()
         return r.future
 
     def close(self, wait: bool = True) -> None:
         with self._cv:
             self._stop = True
+            self._dirty = True
             self._cv.notify()
         if wait:
             self._thread.join()
+            for s in self.slots:
+                s.thread.join()
         if self._error is not None:
             raise self._error
 
@@ -149,19 +212,36 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
-    # ---- dispatch loop ---------------------------------------------------------
+    # ---- dispatch loop (all state below is touched by this thread only) ------
+    def _completed(self, slot, job) -> None:
+        """Called by a worker when its job is done."""
+        with self._cv:
+            self._finished.append((slot, job))
+            self._dirty = True
+            self._cv.notify()
+
     def _loop(self):
         try:
             while True:
                 with self._cv:
-                    if self._stop and not self.pending and not self.running:
-                        return
-                progressed = self._poll()
-                progressed |= self._dispatch()
-                if not progressed:
-                    with self._cv:
-                        if not self._stop or self.pending or self.running:
-                            self._cv.wait(timeout=2e-5 if self.running else 1e-3)
+                    while not self._dirty:
+                        if self._stop and not self.pending and not any(s.busy for s in self.slots):
+                            for s in self.slots:
+                                s.jobs.put(None)
+                            return
+                        self._cv.wait()
+                    self._dirty = False
+                    finished, self._finished = self._finished, []
+                for slot, job in finished:
+                    slot.busy = False
+                    if job.err is None:
+                        job.finish(job.out, job.t_done)
+                    else:
+                        job.fail(job.err, job.t_done)
+                while self._dispatch():
+                    pass
+                if self.pending and not any(s.busy for s in self.slots):
+                    self._unblock()
         except BaseException as exc:  # fail every waiting request, keep the cause
             self._error = exc
             with self._cv:
@@ -170,23 +250,26 @@ class Server:
             for r in rest:
                 if not r.future.done():
                     r.future.set_exception(exc)
+            for s in self.slots:
+                s.jobs.put(None)
 
-    def _poll(self) -> bool:
-        progressed = False
-        still = []
-        for ev, slot, finish in self.running:
-            if ev.query():
-                finish()
-                slot.busy = False
-                progressed = True
-            else:
-                still.append((ev, slot, finish))
-        self.running = still
-        return progressed
-
-    def _pending_scenes(self, exclude=()) -> set[int]:
+    def _unblock(self) -> None:
+        """Nothing runs and nothing waiting was admitted: the oldest request
+        can never be (it needs more memory than the budget frees)."""
         with self._cv:
-            return {r.scene for r in self.pending if r not in exclude}
+            if not self.pending:
+                return
+            r = self.pending[0]
+        self._reject(r, MemoryError(f"a {r.kind} of {r.data.shape[0]} rows does not fit the HBM budget "
+                                    f"({self.budget} bytes)"))
+
+    def _reject(self, r: Request, exc: BaseException) -> None:
+        self._take([r])
+        r.future.set_exception(exc)
+
+    def _pending_scenes(self) -> set[int]:
+        with self._cv:
+            return {r.scene for r in self.pending}
 
     def _admissible(self, r: Request) -> bool:
         res = self.resident.get(r.scene)
@@ -195,7 +278,7 @@ class Server:
         if r.kind == TRACE:
             return res is not None
         if r.kind == REFIT:
-            return res is not None and res.busy == 0 and res.n == r.data.shape[0]
+            return res is not None and res.busy == 0
         return self._make_room(scene_bytes(r.data.shape[0]), keep={r.scene})
 
     def _make_room(self, need: int, keep: set[int]) -> bool:
@@ -232,23 +315,28 @@ class Server:
             res.bvh.close()
 
     def _dispatch(self) -> bool:
+        """Starts one job on a free slot; False when nothing could start."""
         free = [s for s in self.slots if not s.busy]
         if not free:
             return False
         with self._cv:
-            queue = list(self.pending)
-        if not queue:
+            queue_ = list(self.pending)
+        if not queue_:
             return False
         blocked: set[int] = set()
         builds_ahead: set[int] = set()
         chosen = None
-        for r in queue:
+        for r in queue_:
             if r.scene in blocked:
                 continue
             if r.kind != BUILD and r.scene not in self.resident and r.scene not in self.writing \
                     and r.scene not in builds_ahead:
-                self._take([r])
-                r.future.set_exception(KeyError(f"scene {r.scene} is not resident"))
+                self._reject(r, KeyError(f"scene {r.scene} is not resident"))
+                return True
+            if r.kind == REFIT and r.scene not in self.writing and r.scene not in builds_ahead \
+                    and self.resident[r.scene].n != r.data.shape[0]:
+                self._reject(r, ValueError(f"refit of scene {r.scene} with {r.data.shape[0]} triangles; "
+                                           f"it was built with {self.resident[r.scene].n}"))
                 return True
             if self._admissible(r):
                 chosen = r
@@ -261,16 +349,16 @@ class Server:
         slot = free[0]
         if chosen.kind == BUILD:
             group = [chosen]
-            if chosen.data.shape[0] <= self.batch_max_tris:
+            if 2 <= chosen.data.shape[0] <= self.batch_max_tris:
                 seen = {chosen.scene}
-                for r in queue:
+                for r in queue_:
                     if len(group) >= self.batch_max_requests:
                         break
                     if r is chosen or r.kind != BUILD or r.scene in seen or r.scene in blocked:
                         seen.add(r.scene)
                         continue
                     seen.add(r.scene)
-                    if r.data.shape[0] <= self.batch_max_tris and self._admissible(r):
+                    if 2 <= r.data.shape[0] <= self.batch_max_tris and self._admissible(r):
                         group.append(r)
             self._take(group)
             if len(group) > 1:
@@ -288,7 +376,7 @@ class Server:
                 # a trace may run ahead of other traces, never ahead of an
                 # earlier build or refit of its scene
                 stopped = set(blocked)
-                for r in queue:
+                for r in queue_:
                     if r is chosen:
                         continue
                     if r.kind != TRACE:
@@ -313,185 +401,207 @@ class Server:
                 self.pending.remove(r)
                 r.started = now
 
-    def _finish(self, group, results=None) -> None:
-        now = time.perf_counter()
+    def _finish(self, group, t_done: float, results=None) -> None:
         for k, r in enumerate(group):
-            r.done = now
+            r.done = t_done
             self.done.append(r)
             r.future.set_result(None if results is None else results[k])
 
-    def _launch(self, slot, finish) -> None:
-        ev = self.torch.cuda.Event()
-        ev.record(slot.stream)
+    def _fail(self, group, exc: BaseException, t_done: float) -> None:
+        for r in group:
+            r.done = t_done
+            if not r.future.done():
+                r.future.set_exception(exc)
+
+    def _launch(self, slot, work, finish, fail) -> None:
         slot.busy = True
-        self.running.append((ev, slot, finish))
+        slot.jobs.put(_Job(work, finish, fail))
 
-    def _upload(self, slot, key: str, host: np.ndarray):
-        """Host array -> new device tensor, through the slot's pinned buffer,
-        on the slot's stream."""
-        torch = self.torch
-        nbytes = host.nbytes
-        pin = slot.pinned_buffer(torch, key, nbytes)
-        pin.numpy()[:nbytes] = host.reshape(-1).view(np.uint8)
-        with torch.cuda.stream(slot.stream):
-            dev = torch.empty(host.shape, dtype=torch.float32, device=self.device)
-            dev.view(torch.uint8).view(-1).copy_(pin, non_blocking=True)
-        return dev
-
-    def _check(self, slot, status: int) -> None:
-        slot.ctx.check(status)
-
-    # ---- jobs ------------------------------------------------------------------
+    # ---- jobs: bookkeeping here, GPU work in the slot's worker -----------------
     def _start_build(self, slot, r: Request) -> None:
-        from . import _lib
-
         n = r.data.shape[0]
-        self.used += scene_bytes(n)
+        nbytes = scene_bytes(n)
+        self.used += nbytes
         self.writing.add(r.scene)
-        dev = self._upload(slot, "tris", r.data)
-        bvh = lbapi.BVH(slot.ctx)
-        self._check(slot, _lib.lib().lbvh_build_triangles(slot.ctx.handle, dev.data_ptr(), n, 0, bvh.handle))
-        # the traversal copy is made here, on this stream, so that traces on
-        # other streams never build it concurrently
-        self._check(slot, _lib.lib().lbvh_bvh_prepare_trace(slot.ctx.handle, bvh.handle))
-        bvh.kind = lbapi.TRIANGLES
+        L, ctx = _lib.lib(), slot.ctx
 
-        def finish():
+        def work():
+            dev = slot.upload(r.data, 12)
+            bvh = lbapi.BVH(ctx)
+            ctx.check(L.lbvh_build_triangles(ctx.handle, dev.data_ptr(), n, 0, bvh.handle))
+            # the traversal copy is made here, on this stream, so that traces
+            # on other streams never build it concurrently
+            ctx.check(L.lbvh_bvh_prepare_trace(ctx.handle, bvh.handle))
+            bvh.kind = lbapi.TRIANGLES
+            return bvh, dev
+
+        def finish(out, t):
+            bvh, dev = out
             self._drop(r.scene)
-            self.resident[r.scene] = Resident(n, scene_bytes(n), bvh=bvh, tris=dev, last_use=time.perf_counter())
+            self.resident[r.scene] = Resident(n, nbytes, bvh=bvh, tris=dev, last_use=t)
             self.writing.discard(r.scene)
-            self._finish([r])
+            self._finish([r], t)
 
-        self._launch(slot, finish)
+        def fail(exc, t):
+            self.used -= nbytes
+            self.writing.discard(r.scene)
+            self._fail([r], exc, t)
+
+        self._launch(slot, work, finish, fail)
 
     def _start_batch_build(self, slot, group) -> None:
-        from . import _lib
-
         counts = np.array([r.data.shape[0] for r in group], np.int64)
         offsets = np.zeros(len(group) + 1, np.uint32)
         offsets[1:] = np.cumsum(counts)
-        for r in group:
-            self.used += scene_bytes(r.data.shape[0])
+        sizes = [scene_bytes(int(c)) for c in counts]
+        for r, b in zip(group, sizes):
+            self.used += b
             self.writing.add(r.scene)
-        dev = self._upload(slot, "tris", np.concatenate([r.data for r in group]))
-        batch = lbapi.Batch(slot.ctx)
-        self._check(slot, _lib.lib().lbvh_batch_build_triangles(slot.ctx.handle, dev.data_ptr(), int(offsets[-1]),
-                                                               offsets.ctypes.data, len(group), batch._h))
-        self._check(slot, _lib.lib().lbvh_batch_prepare_trace(slot.ctx.handle, batch._h))
-        batch._keep = (dev, offsets)
-        batch._offsets = offsets
-        ref = _BatchRef(batch, dev, offsets, members=len(group))
+        L, ctx, torch = _lib.lib(), slot.ctx, self.torch
 
-        def finish():
-            now = time.perf_counter()
+        def work():
+            dev = torch.empty((int(offsets[-1]), 12), dtype=torch.float32, device=self.device)
             for k, r in enumerate(group):
+                dev[int(offsets[k]) : int(offsets[k + 1])].copy_(torch.from_numpy(r.data), non_blocking=True)
+            batch = lbapi.Batch(ctx)
+            ctx.check(L.lbvh_batch_build_triangles(ctx.handle, dev.data_ptr(), int(offsets[-1]),
+                                                   offsets.ctypes.data, len(group), batch._h))
+            ctx.check(L.lbvh_batch_prepare_trace(ctx.handle, batch._h))
+            batch._keep = (dev, offsets)
+            batch._offsets = offsets
+            return batch, dev
+
+        def finish(out, t):
+            batch, dev = out
+            ref = _BatchRef(batch, dev, offsets, members=len(group))
+            for k, (r, b) in enumerate(zip(group, sizes)):
                 self._drop(r.scene)
-                n = r.data.shape[0]
-                self.resident[r.scene] = Resident(n, scene_bytes(n), batch=ref, index=k, last_use=now)
+                self.resident[r.scene] = Resident(r.data.shape[0], b, batch=ref, index=k, last_use=t)
                 self.writing.discard(r.scene)
-            self._finish(group)
+            self._finish(group, t)
 
-        self._launch(slot, finish)
+        def fail(exc, t):
+            for r, b in zip(group, sizes):
+                self.used -= b
+                self.writing.discard(r.scene)
+            self._fail(group, exc, t)
 
-    def _standalone(self, slot, scene: int) -> Resident:
-        """Moves a batch member into its own BVH (same nodes), for a refit."""
-        res = self.resident[scene]
-        ref, k = res.batch, res.index
-        o = ref.offsets
-        nodes = ref.batch.mesh_nodes(k)
-        tris = ref.tris[int(o[k]) : int(o[k + 1])]
-        bvh = lbapi.BVH.from_nodes(nodes, tris, slot.ctx)
-        res.retired = True  # the batch member leaves; its traces have finished (refits need busy == 0)
-        ref.members -= 1
-        if ref.members == 0:
-            ref.batch.close()
-        new = Resident(res.n, res.nbytes, bvh=bvh, tris=tris, busy=res.busy, last_use=res.last_use)
-        self.resident[scene] = new
-        return new
+        self._launch(slot, work, finish, fail)
 
     def _start_refit(self, slot, r: Request) -> None:
-        from . import _lib
-
+        """A batch member is first moved into its own BVH (the same nodes,
+        copied on the device), then refitted."""
         res = self.resident[r.scene]
-        if res.batch is not None:
-            res = self._standalone(slot, r.scene)
         self.writing.add(r.scene)
-        dev = self._upload(slot, "tris", r.data)
-        self._check(slot, _lib.lib().lbvh_refit_triangles(slot.ctx.handle, res.bvh.handle, dev.data_ptr()))
-        self._check(slot, _lib.lib().lbvh_bvh_prepare_trace(slot.ctx.handle, res.bvh.handle))
+        L, ctx, torch = _lib.lib(), slot.ctx, self.torch
+        ref, k = res.batch, res.index
 
-        def finish():
-            res.tris = dev  # the refitted BVH now borrows these triangles
-            res.last_use = time.perf_counter()
+        def work():
+            bvh = res.bvh
+            if ref is not None:
+                o = ref.offsets
+                total_nodes = int(o[-1]) - (o.size - 1)
+                all_nodes = torch.empty((total_nodes, 8), dtype=torch.float32, device=self.device)
+                ctx.check(L.lbvh_batch_nodes(ctx.handle, ref.batch._h, all_nodes.data_ptr()))
+                start = int(o[k]) - k
+                nodes = all_nodes[start : start + int(o[k + 1] - o[k]) - 1]
+                bvh = lbapi.BVH.from_nodes(nodes, ref.tris[int(o[k]) : int(o[k + 1])], ctx)
+            dev = slot.upload(r.data, 12)
+            ctx.check(L.lbvh_refit_triangles(ctx.handle, bvh.handle, dev.data_ptr()))
+            ctx.check(L.lbvh_bvh_prepare_trace(ctx.handle, bvh.handle))
+            return bvh, dev
+
+        def finish(out, t):
+            bvh, dev = out
+            if ref is not None:  # the member leaves its batch
+                ref.members -= 1
+                if ref.members == 0:
+                    ref.batch.close()
+                cur = Resident(res.n, res.nbytes, bvh=bvh, tris=dev, last_use=t)
+                self.resident[r.scene] = cur
+            else:
+                res.tris = dev  # the refitted BVH now borrows these triangles
+                res.last_use = t
             self.resident.move_to_end(r.scene)
             self.writing.discard(r.scene)
-            self._finish([r])
+            self._finish([r], t)
 
-        self._launch(slot, finish)
+        def fail(exc, t):
+            # the tree may be half refitted: the scene leaves residency
+            self.writing.discard(r.scene)
+            self._drop(r.scene)
+            self._fail([r], exc, t)
+
+        self._launch(slot, work, finish, fail)
 
     def _start_trace(self, slot, group) -> None:
-        from . import _lib
-
         torch = self.torch
-        res0 = self.resident[group[0].scene]
         used = [self.resident[r.scene] for r in group]
         for res in used:
             res.busy += 1
+        res0 = used[0]
+        L, ctx = _lib.lib(), slot.ctx
         if res0.batch is None:
-            r = group[0]
-            m = r.data.shape[0]
-            rays = self._upload(slot, "rays", r.data)
-            with torch.cuda.stream(slot.stream):
-                hits = torch.empty((m, 4), dtype=torch.float32, device=self.device)
-            self._check(slot, _lib.lib().lbvh_trace_triangles(slot.ctx.handle, res0.bvh.handle, rays.data_ptr(), m,
-                                                             hits.data_ptr()))
+            m = group[0].data.shape[0]
             spans = [(0, m)]
+            roff = None
         else:
             ref = res0.batch
             nm = ref.offsets.size - 1
-            order = sorted(range(len(group)), key=lambda k: self.resident[group[k].scene].index)
+            order = sorted(range(len(group)), key=lambda k: used[k].index)
             per_mesh = np.zeros(nm, np.int64)
             for k in order:
-                per_mesh[self.resident[group[k].scene].index] += group[k].data.shape[0]
+                per_mesh[used[k].index] += group[k].data.shape[0]
             roff = np.zeros(nm + 1, np.uint32)
             roff[1:] = np.cumsum(per_mesh)
-            cursor = roff[:-1].astype(np.int64).copy()
+            cursor = roff[:-1].astype(np.int64)
             spans = [None] * len(group)
-            chunks = [None] * len(group)
             for k in order:
-                idx = self.resident[group[k].scene].index
-                m_k = group[k].data.shape[0]
-                spans[k] = (int(cursor[idx]), int(cursor[idx]) + m_k)
-                cursor[idx] += m_k
-            allr = np.empty((int(roff[-1]), 8), np.float32)
-            for k, r in enumerate(group):
-                allr[spans[k][0] : spans[k][1]] = r.data
-            m = allr.shape[0]
-            rays = self._upload(slot, "rays", allr)
-            with torch.cuda.stream(slot.stream):
-                hits = torch.empty((m, 4), dtype=torch.float32, device=self.device)
-            self._check(slot, _lib.lib().lbvh_batch_trace_triangles(slot.ctx.handle, ref.batch._h, rays.data_ptr(),
-                                                                   roff.ctypes.data, m, hits.data_ptr()))
-        pin = slot.pinned_buffer(torch, "hits", 16 * m)
-        with torch.cuda.stream(slot.stream):
-            pin.copy_(hits.view(torch.uint8).view(-1), non_blocking=True)
+                idx = used[k].index
+                spans[k] = (int(cursor[idx]), int(cursor[idx]) + group[k].data.shape[0])
+                cursor[idx] += group[k].data.shape[0]
+            m = int(roff[-1])
 
-        def finish():
-            _ = (rays, hits)  # keep the device buffers alive until the GPU is done
-            all_hits = pin.numpy().view(lbapi.HIT_DTYPE)
-            results = [np.array(all_hits[a:b]) for a, b in spans]
-            now = time.perf_counter()
+        def work():
+            rays = torch.empty((m, 8), dtype=torch.float32, device=self.device)
+            for (a, b), r in zip(spans, group):
+                rays[a:b].copy_(torch.from_numpy(r.data), non_blocking=True)
+            hits = torch.empty((m, 4), dtype=torch.float32, device=self.device)
+            if m == 0:
+                pass
+            elif roff is None:
+                ctx.check(L.lbvh_trace_triangles(ctx.handle, res0.bvh.handle, rays.data_ptr(), m, hits.data_ptr()))
+            else:
+                ctx.check(L.lbvh_batch_trace_triangles(ctx.handle, res0.batch.batch._h, rays.data_ptr(),
+                                                       roff.ctypes.data, m, hits.data_ptr()))
+            outs = []
+            for a, b in spans:  # mapped while the trace runs
+                out = np.empty(b - a, lbapi.HIT_DTYPE)
+                _touch(out)
+                outs.append(out)
+            for (a, b), out in zip(spans, outs):
+                torch.from_numpy(out.view(np.float32).reshape(-1, 4)).copy_(hits[a:b], non_blocking=True)
+            return outs
+
+        def settle(t):
             for r, res in zip(group, used):
                 res.busy -= 1
-                res.last_use = now
+                res.last_use = t
                 if res.retired:
                     if res.busy == 0:
                         self._release(res)
                 elif r.scene in self.resident:
                     self.resident.move_to_end(r.scene)
-            self._finish(group, results)
 
-        self._launch(slot, finish)
+        def finish(outs, t):
+            settle(t)
+            self._finish(group, t, outs)
+
+        def fail(exc, t):
+            settle(t)
+            self._fail(group, exc, t)
+
+        self._launch(slot, work, finish, fail)
 
 
 def run_plain(requests, device: int = 0):

@@ -68,3 +68,20 @@ def test_trace_of_unknown_scene_fails_cleanly(lib_built):
         srv.submit("build", 1, t).result(timeout=30)
         hits = srv.submit("trace", 1, scenes.incoherent_rays(t, 500, 2)).result(timeout=30)
         assert hits.shape == (500,)
+
+
+def test_rejected_requests_leave_the_server_usable(lib_built):
+    t = scenes.soup(1000, 3)
+    with Server(slots=2, hbm_budget=scene_bytes(1000) + 1024) as srv:
+        srv.submit("build", 1, t).result(timeout=30)
+        with pytest.raises(ValueError):  # a refit keeps the triangle count
+            srv.submit("refit", 1, t[:999]).result(timeout=30)
+        hits = srv.submit("trace", 1, np.zeros((0, 8), np.float32)).result(timeout=30)
+        assert hits.shape == (0,)
+        with pytest.raises(MemoryError):  # larger than the whole budget
+            srv.submit("build", 2, scenes.soup(5000, 4)).result(timeout=30)
+        srv.submit("build", 3, t).result(timeout=30)
+        rays = scenes.incoherent_rays(t, 300, 5)
+        got = srv.submit("trace", 3, rays).result(timeout=30)
+    want = run_plain([(0.0, "build", 3, t), (0.0, "trace", 3, rays)])[1][0]
+    assert hit_mismatches(got, want).size == 0
