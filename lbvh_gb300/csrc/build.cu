@@ -233,7 +233,7 @@ block_excl_scan_256(uint32_t v, uint32_t* s_warp)
 }
 
 template<bool kPairs, bool kIotaVals>
-__global__ __launch_bounds__(kSortThreads) void
+__global__ __launch_bounds__(kSortThreads, kPairs ? 3 : 4) void
 k_onesweep(const uint32_t* __restrict__ kin,
            uint32_t* __restrict__ kout,
            const uint32_t* __restrict__ vin,
@@ -262,26 +262,25 @@ k_onesweep(const uint32_t* __restrict__ kin,
   const uint32_t base = tile * uint32_t(kSortTile);
   const uint32_t shift = pass * 8;
 
-  uint32_t key[kSortItems], val[kPairs ? kSortItems : 1], dig[kSortItems], rank[kSortItems];
+  // digits are recomputed from the keys where needed (fewer live registers)
+  const uint32_t first = base + uint32_t(warp) * (32 * kSortItems) + lane;
+  auto digit = [&](uint32_t kv, int k) -> uint32_t {
+    return first + uint32_t(k) * 32 < n ? (kv >> shift) & 255u : 256u; // 256: not a key, in no bucket
+  };
+  uint32_t key[kSortItems], val[kPairs ? kSortItems : 1], rank[kSortItems];
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
-    const uint32_t idx = base + uint32_t(warp) * (32 * kSortItems) + uint32_t(k) * 32 + lane;
-    if (idx < n) {
-      key[k] = kin[idx];
-      if (kPairs)
-        val[kPairs ? k : 0] = kIotaVals ? idx : vin[idx];
-      dig[k] = (key[k] >> shift) & 255u;
-    } else {
-      key[k] = 0;
-      dig[k] = 256; // not a key: ranked in no bucket
-    }
+    const uint32_t idx = first + uint32_t(k) * 32;
+    key[k] = idx < n ? kin[idx] : 0u;
+    if (kPairs)
+      val[kPairs ? k : 0] = idx < n ? (kIotaVals ? idx : vin[idx]) : 0u;
   }
 
   // warp-level stable ranking: items in (k, lane) order are in index order
   const uint32_t lt_mask = (1u << lane) - 1u;
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
-    const uint32_t d = dig[k];
+    const uint32_t d = digit(key[k], k);
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
     const uint32_t pre = __popc(peers & lt_mask);
     uint32_t before = 0;
@@ -356,7 +355,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
   // reorder the tile in shared memory by digit
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
-    const uint32_t d = dig[k];
+    const uint32_t d = digit(key[k], k);
     if (d < 256) {
       const uint32_t pos = s_tile_start[d] + s_whist[warp][d] + rank[k];
       s_keys[pos] = key[k];

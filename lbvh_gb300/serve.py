@@ -11,10 +11,13 @@ at a time):
   least-recently-used resident scenes that no queued or running request
   needs, and otherwise waits until running work frees memory;
 * small builds (at most `batch_max_tris` triangles) waiting together are
-  coalesced into one batched build (lbvh_batch_build_triangles), and small
-  traces against scenes of the same batch into one batched trace;
+  coalesced into one batched build (lbvh_batch_build_triangles); small
+  traces queued together against one tree become one trace launch, and those
+  against scenes of the same batch one batched trace;
 * requests on one scene keep their submission order (a trace submitted after
   a refit sees the refitted tree); requests on different scenes overlap.
+  Waiting requests sit in one queue per scene, so choosing the next job
+  costs time in the number of scenes, not of waiting requests.
 
 Host data moves straight between the caller's (pageable) arrays and the
 device, each request's copy issued by the worker that runs it: on a
@@ -57,6 +60,7 @@ class Request:
     future: Future = field(default_factory=Future)
     started: float = 0.0
     done: float = 0.0
+    seq: int = 0
 
 
 @dataclass(eq=False)
@@ -166,7 +170,12 @@ class Server:
         self.trace_batch_max_rays = trace_batch_max_rays
         self.resident: "collections.OrderedDict[int, Resident]" = collections.OrderedDict()
         self.writing: set[int] = set()        # scenes with a running build / refit
-        self.pending: collections.deque[Request] = collections.deque()
+        self._inbox: list[Request] = []       # submitted, not yet queued (guarded by _cv)
+        self._seq = 0                         # submission counter (guarded by _cv)
+        # waiting requests, one FIFO per scene (dispatch thread only): a
+        # dispatch looks at the scenes' oldest requests, so its cost grows
+        # with the number of scenes, not with the number of waiting requests
+        self.queues: dict[int, collections.deque[Request]] = {}
         self.done: list[Request] = []
         self.evictions = 0
         self.coalesced = 0
@@ -189,7 +198,9 @@ class Server:
         with self._cv:
             if self._stop:
                 raise RuntimeError("server is closed")
-            self.pending.append(r)
+            r.seq = self._seq
+            self._seq += 1
+            self._inbox.append(r)
             self._dirty = True
             self._cv.notify()
         return r.future
@@ -225,13 +236,19 @@ class Server:
             while True:
                 with self._cv:
                     while not self._dirty:
-                        if self._stop and not self.pending and not any(s.busy for s in self.slots):
+                        if self._stop and not self.queues and not any(s.busy for s in self.slots):
                             for s in self.slots:
                                 s.jobs.put(None)
                             return
                         self._cv.wait()
                     self._dirty = False
                     finished, self._finished = self._finished, []
+                    inbox, self._inbox = self._inbox, []
+                for r in inbox:
+                    q = self.queues.get(r.scene)
+                    if q is None:
+                        q = self.queues[r.scene] = collections.deque()
+                    q.append(r)
                 for slot, job in finished:
                     slot.busy = False
                     if job.err is None:
@@ -240,13 +257,15 @@ class Server:
                         job.fail(job.err, job.t_done)
                 while self._dispatch():
                     pass
-                if self.pending and not any(s.busy for s in self.slots):
+                if self.queues and not any(s.busy for s in self.slots):
                     self._unblock()
         except BaseException as exc:  # fail every waiting request, keep the cause
             self._error = exc
             with self._cv:
-                rest = list(self.pending)
-                self.pending.clear()
+                rest = self._inbox
+                self._inbox = []
+            rest += [r for q in self.queues.values() for r in q]
+            self.queues.clear()
             for r in rest:
                 if not r.future.done():
                     r.future.set_exception(exc)
@@ -256,10 +275,9 @@ class Server:
     def _unblock(self) -> None:
         """Nothing runs and nothing waiting was admitted: the oldest request
         can never be (it needs more memory than the budget frees)."""
-        with self._cv:
-            if not self.pending:
-                return
-            r = self.pending[0]
+        if not self.queues:
+            return
+        r = min((q[0] for q in self.queues.values()), key=lambda x: x.seq)
         self._reject(r, MemoryError(f"a {r.kind} of {r.data.shape[0]} rows does not fit the HBM budget "
                                     f"({self.budget} bytes)"))
 
@@ -268,8 +286,7 @@ class Server:
         r.future.set_exception(exc)
 
     def _pending_scenes(self) -> set[int]:
-        with self._cv:
-            return {r.scene for r in self.pending}
+        return set(self.queues)
 
     def _admissible(self, r: Request) -> bool:
         res = self.resident.get(r.scene)
@@ -315,50 +332,40 @@ class Server:
             res.bvh.close()
 
     def _dispatch(self) -> bool:
-        """Starts one job on a free slot; False when nothing could start."""
+        """Starts one job on a free slot; False when nothing could start.
+        Candidates are each scene's oldest waiting request (oldest scene
+        first) and, for a trace, the run of traces queued right behind it,
+        so a scene's requests start in submission order."""
         free = [s for s in self.slots if not s.busy]
-        if not free:
+        if not free or not self.queues:
             return False
-        with self._cv:
-            queue_ = list(self.pending)
-        if not queue_:
-            return False
-        blocked: set[int] = set()
-        builds_ahead: set[int] = set()
+        heads = sorted(self.queues.items(), key=lambda kv: kv[1][0].seq)
         chosen = None
-        for r in queue_:
-            if r.scene in blocked:
-                continue
-            if r.kind != BUILD and r.scene not in self.resident and r.scene not in self.writing \
-                    and r.scene not in builds_ahead:
-                self._reject(r, KeyError(f"scene {r.scene} is not resident"))
+        for scene, q in heads:
+            r = q[0]
+            res = self.resident.get(scene)
+            if r.kind != BUILD and res is None and scene not in self.writing:
+                self._reject(r, KeyError(f"scene {scene} is not resident"))
                 return True
-            if r.kind == REFIT and r.scene not in self.writing and r.scene not in builds_ahead \
-                    and self.resident[r.scene].n != r.data.shape[0]:
-                self._reject(r, ValueError(f"refit of scene {r.scene} with {r.data.shape[0]} triangles; "
-                                           f"it was built with {self.resident[r.scene].n}"))
+            if r.kind == REFIT and scene not in self.writing and res.n != r.data.shape[0]:
+                self._reject(r, ValueError(f"refit of scene {scene} with {r.data.shape[0]} triangles; "
+                                           f"it was built with {res.n}"))
                 return True
             if self._admissible(r):
                 chosen = r
                 break
-            blocked.add(r.scene)
-            if r.kind == BUILD:
-                builds_ahead.add(r.scene)
         if chosen is None:
             return False
         slot = free[0]
         if chosen.kind == BUILD:
             group = [chosen]
             if 2 <= chosen.data.shape[0] <= self.batch_max_tris:
-                seen = {chosen.scene}
-                for r in queue_:
+                for scene, q in heads:
                     if len(group) >= self.batch_max_requests:
                         break
-                    if r is chosen or r.kind != BUILD or r.scene in seen or r.scene in blocked:
-                        seen.add(r.scene)
-                        continue
-                    seen.add(r.scene)
-                    if 2 <= r.data.shape[0] <= self.batch_max_tris and self._admissible(r):
+                    r = q[0]
+                    if r is not chosen and r.kind == BUILD and 2 <= r.data.shape[0] <= self.batch_max_tris \
+                            and self._admissible(r):
                         group.append(r)
             self._take(group)
             if len(group) > 1:
@@ -371,35 +378,49 @@ class Server:
             self._start_refit(slot, chosen)
         else:
             res = self.resident[chosen.scene]
-            group = [chosen]
-            if res.batch is not None and chosen.data.shape[0] <= self.trace_batch_max_rays:
-                # a trace may run ahead of other traces, never ahead of an
-                # earlier build or refit of its scene
-                stopped = set(blocked)
-                for r in queue_:
-                    if r is chosen:
+            group = self._trace_run(chosen.scene, [chosen])
+            if res.batch is not None and len(group) < self.batch_max_requests \
+                    and chosen.data.shape[0] <= self.trace_batch_max_rays:
+                for scene, q in heads:
+                    other = self.resident.get(scene)
+                    if scene == chosen.scene or other is None or other.batch is not res.batch \
+                            or scene in self.writing or q[0].kind != TRACE \
+                            or q[0].data.shape[0] > self.trace_batch_max_rays:
                         continue
-                    if r.kind != TRACE:
-                        stopped.add(r.scene)
-                        continue
-                    if r.scene in stopped:
-                        continue
-                    other = self.resident.get(r.scene)
-                    if other is not None and other.batch is res.batch and r.scene not in self.writing \
-                            and r.data.shape[0] <= self.trace_batch_max_rays:
-                        group.append(r)
+                    group = self._trace_run(scene, group + [q[0]])
+                    if len(group) >= self.batch_max_requests:
+                        break
             self._take(group)
             if len(group) > 1:
                 self.coalesced += len(group)
             self._start_trace(slot, group)
         return True
 
+    def _trace_run(self, scene: int, group: list) -> list:
+        """Extends a group ending with the head of `scene`'s queue by the small
+        traces queued right behind it (they read the same tree)."""
+        if group[-1].data.shape[0] > self.trace_batch_max_rays:
+            return group
+        q = self.queues[scene]
+        for k in range(1, len(q)):
+            r = q[k]
+            if len(group) >= self.batch_max_requests or r.kind != TRACE \
+                    or r.data.shape[0] > self.trace_batch_max_rays:
+                break
+            group.append(r)
+        return group
+
     def _take(self, group) -> None:
+        """Removes a group from the queues: for each scene it is a run from
+        the front of the scene's queue, in queue order."""
         now = time.perf_counter()
-        with self._cv:
-            for r in group:
-                self.pending.remove(r)
-                r.started = now
+        for r in group:
+            q = self.queues[r.scene]
+            assert q[0] is r
+            q.popleft()
+            if not q:
+                del self.queues[r.scene]
+            r.started = now
 
     def _finish(self, group, t_done: float, results=None) -> None:
         for k, r in enumerate(group):
@@ -541,9 +562,10 @@ class Server:
             res.busy += 1
         res0 = used[0]
         L, ctx = _lib.lib(), slot.ctx
-        if res0.batch is None:
-            m = group[0].data.shape[0]
-            spans = [(0, m)]
+        if res0.batch is None:  # traces of one tree, one after another
+            ends = np.cumsum([r.data.shape[0] for r in group])
+            spans = [(int(e - r.data.shape[0]), int(e)) for r, e in zip(group, ends)]
+            m = int(ends[-1])
             roff = None
         else:
             ref = res0.batch
