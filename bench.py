@@ -115,6 +115,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(inside)}
 
 
+def replica_throughput(step_ms: float, units: int, world: int, device=None):
+    """Whole-job throughput of `world` independent replicas, each
+    processing `units` per step: the slowest rank's step time (max over
+    ranks) and units x world / that time, in millions per second."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([step_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    return step_ms, world * units / (step_ms * 1e-3) / 1e6
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -492,12 +506,8 @@ def main():
     build_ms = [a.elapsed_time(b) for a, b, _ in ev]
     trace_ms = [b.elapsed_time(c) for _, b, c in ev]
     step_ms = float(np.mean([x + y for x, y in zip(build_ms, trace_ms)]))
-    if world > 1:
-        t = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = world * m / (step_ms * 1e-3) / 1e6
-    gpu_launches = args.steps * (8 + 2)  # bounds, Morton, 4 sort passes, split, fit; repack, trace
+    step_ms, value = replica_throughput(step_ms, m, world, dev)
+    gpu_launches = args.steps * (8 + 2)  # bounds, Morton, 4 sort passes, local + global tree; repack, trace
 
     # correctness guard on the timed output: the same hits as an untimed run
     ref_hits = torch.empty_like(hits)
