@@ -52,7 +52,9 @@ typedef enum lbvh_status
   LBVH_ERR_OOM = 2,         /* device allocation failed */
   LBVH_ERR_TIMEOUT = 3,     /* a bounded device-side wait expired */
   LBVH_ERR_DEVICE = 4,      /* CUDA runtime error; see lbvh_ctx_last_error */
-  LBVH_ERR_BAD_TOPOLOGY = 5 /* a node array that is not a binary tree */
+  LBVH_ERR_BAD_TOPOLOGY = 5, /* a node array that is not a binary tree */
+  LBVH_ERR_NOT_RESIDENT = 6, /* server: a trace or refit of a scene it does not hold */
+  LBVH_ERR_BUDGET = 7        /* server: a build larger than the whole HBM budget */
 } lbvh_status;
 
 typedef struct lbvh_ctx lbvh_ctx; /* device, stream, workspace */
@@ -211,6 +213,9 @@ LBVH_API int lbvh_batch_info(const lbvh_batch* batch, size_t* n_meshes, size_t* 
 LBVH_API int lbvh_batch_prepare_trace(lbvh_ctx* ctx, lbvh_batch* batch);
 /* Copies all node blocks (total_prims - n_meshes nodes of 32 bytes). */
 LBVH_API int lbvh_batch_nodes(lbvh_ctx* ctx, const lbvh_batch* batch, void* dst);
+/* Copies mesh k's node block (its triangle count - 1 nodes), which is the node
+ * array the reference's builder makes for that mesh alone. */
+LBVH_API int lbvh_batch_mesh_nodes(lbvh_ctx* ctx, const lbvh_batch* batch, size_t k, void* dst);
 /* Traces rays [ray_offsets[k], ray_offsets[k + 1]) against mesh k (m rays in
  * all, n_meshes + 1 offsets); hit primitive ids are mesh-local. Host ray
  * offsets are staged in the context, so once lbvh_batch_prepare_trace has
@@ -245,6 +250,75 @@ LBVH_API int lbvh_batch_trace_triangles(lbvh_ctx* ctx, const lbvh_batch* batch, 
  * race and corrupt each other, so serialize them per device. */
 LBVH_API int lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint32_t* d_status,
                                           void* stream);
+
+/* ---- Request server -------------------------------------------------------
+ * No reference counterpart (the reference builds and traces one scene per
+ * call). A server keeps BVHs resident on one GPU and runs build / refit /
+ * trace requests as they arrive: one dispatch thread and `slots` worker
+ * threads, each worker with its own stream and context, so requests admitted
+ * while others run overlap on the device. Admission is against an HBM budget
+ * with least-recently-used eviction of scenes no waiting or running request
+ * needs; builds of at most batch_max_tris triangles that wait together are
+ * coalesced into one batched build, small traces (at most
+ * trace_batch_max_rays rays) of one tree into one launch and of one batch
+ * into one batched trace. A scene's requests start in submission order.
+ * Every result equals the same request run alone through lbvh_build_triangles
+ * / lbvh_refit_triangles / lbvh_trace_triangles. */
+typedef struct lbvh_server lbvh_server;
+
+#define LBVH_REQ_BUILD 0 /* data: rows triangles (n x 12 float32); (re)builds the scene */
+#define LBVH_REQ_REFIT 1 /* data: the scene's triangles moved (same count and order) */
+#define LBVH_REQ_TRACE 2 /* data: rows rays (n x 8 float32); hits: rows lbvh_hit */
+
+typedef struct lbvh_server_config
+{
+  int device;
+  int slots;                   /* worker streams (1..64) */
+  size_t hbm_budget;           /* bytes of resident scenes: 144 per triangle + 64 KiB each */
+  size_t batch_max_tris;       /* largest build that is coalesced (0: never) */
+  size_t batch_max_requests;   /* most requests in one coalesced launch */
+  size_t trace_batch_max_rays; /* largest trace that is coalesced */
+} lbvh_server_config;
+
+typedef struct lbvh_request_done
+{
+  uint64_t ticket;
+  int status;                  /* lbvh_status of the request */
+  int kind;                    /* LBVH_REQ_* */
+  int64_t scene;
+  double arrival;              /* seconds since the server started: submitted */
+  double start;                /* dispatched to a worker */
+  double done;                 /* its GPU work and result copy finished */
+  char message[160];           /* why it failed ("" on success) */
+} lbvh_request_done;
+
+typedef struct lbvh_server_stats
+{
+  uint64_t submitted, completed, coalesced_requests, evictions;
+  uint64_t resident_scenes, resident_bytes;
+} lbvh_server_stats;
+
+LBVH_API int lbvh_server_create(const lbvh_server_config* config, lbvh_server** out);
+/* Queues a request. `data` (host or device) must stay valid and unchanged,
+ * and `hits` (trace only: rows lbvh_hit, host or device) writable, until the
+ * request is reported done. Returns its ticket. */
+LBVH_API int lbvh_server_submit(lbvh_server* server, int kind, int64_t scene, const float* data, size_t rows,
+                                void* hits, uint64_t* ticket);
+/* Waits up to timeout_s seconds for finished requests and moves up to `max`
+ * of them into out (each request is reported once); *n_out = how many. */
+LBVH_API int lbvh_server_wait_any(lbvh_server* server, lbvh_request_done* out, size_t max, double timeout_s,
+                                  size_t* n_out);
+/* The server's clock: seconds since it was created (the clock of
+ * lbvh_request_done's times). */
+LBVH_API double lbvh_server_clock(const lbvh_server* server);
+/* Blocks until every request submitted so far has finished. */
+LBVH_API int lbvh_server_drain(lbvh_server* server);
+LBVH_API int lbvh_server_stats_get(lbvh_server* server, lbvh_server_stats* out);
+/* The scenes resident after the dispatcher's last step (up to cap ids). */
+LBVH_API int lbvh_server_resident(lbvh_server* server, int64_t* scenes, size_t cap, size_t* n_out);
+/* Finishes all queued work, stops the threads and frees every resident
+ * scene. Finished requests not yet taken by lbvh_server_wait_any are lost. */
+LBVH_API int lbvh_server_destroy(lbvh_server* server);
 
 #ifdef __cplusplus
 } /* extern "C" */

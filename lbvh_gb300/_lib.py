@@ -19,6 +19,10 @@ LBVH_ERR_OOM = 2
 LBVH_ERR_TIMEOUT = 3
 LBVH_ERR_DEVICE = 4
 LBVH_ERR_BAD_TOPOLOGY = 5
+LBVH_ERR_NOT_RESIDENT = 6
+LBVH_ERR_BUDGET = 7
+
+REQ_BUILD, REQ_REFIT, REQ_TRACE = 0, 1, 2
 
 NOALLOC_MAX_PRIMS = 65536
 PARAM_TRACE_BLOCKS_PER_SM = 1
@@ -68,7 +72,36 @@ SIGNATURES = {
     "lbvh_batch_info": (_I, [_P, ctypes.POINTER(_S), ctypes.POINTER(_S), ctypes.POINTER(_S)]),
     "lbvh_batch_nodes": (_I, [_P, _P, _P]),
     "lbvh_batch_trace_triangles": (_I, [_P, _P, _P, _P, _S, _P]),
+    "lbvh_batch_mesh_nodes": (_I, [_P, _P, _S, _P]),
+    "lbvh_server_create": (_I, [_P, _PP]),
+    "lbvh_server_submit": (_I, [_P, _I, ctypes.c_int64, _P, _S, _P, ctypes.POINTER(ctypes.c_uint64)]),
+    "lbvh_server_wait_any": (_I, [_P, _P, _S, ctypes.c_double, ctypes.POINTER(_S)]),
+    "lbvh_server_drain": (_I, [_P]),
+    "lbvh_server_clock": (ctypes.c_double, [_P]),
+    "lbvh_server_stats_get": (_I, [_P, _P]),
+    "lbvh_server_resident": (_I, [_P, _P, _S, ctypes.POINTER(_S)]),
+    "lbvh_server_destroy": (_I, [_P]),
 }
+
+
+class ServerConfig(ctypes.Structure):
+    """lbvh_server_config"""
+    _fields_ = [("device", _I), ("slots", _I), ("hbm_budget", _S), ("batch_max_tris", _S),
+                ("batch_max_requests", _S), ("trace_batch_max_rays", _S)]
+
+
+class RequestDone(ctypes.Structure):
+    """lbvh_request_done"""
+    _fields_ = [("ticket", ctypes.c_uint64), ("status", _I), ("kind", _I), ("scene", ctypes.c_int64),
+                ("arrival", ctypes.c_double), ("start", ctypes.c_double), ("done", ctypes.c_double),
+                ("message", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    """lbvh_server_stats"""
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("coalesced_requests", ctypes.c_uint64), ("evictions", ctypes.c_uint64),
+                ("resident_scenes", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64)]
 
 
 class LbvhError(RuntimeError):

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 using namespace lbvh_gb300;
 
@@ -423,6 +424,10 @@ lbvh_status_string(int s)
       return "CUDA error";
     case LBVH_ERR_BAD_TOPOLOGY:
       return "malformed tree";
+    case LBVH_ERR_NOT_RESIDENT:
+      return "scene not resident";
+    case LBVH_ERR_BUDGET:
+      return "larger than the HBM budget";
     default:
       return "unknown status";
   }
@@ -855,6 +860,7 @@ struct lbvh_batch
   DevBuf nodes;              // total - n_meshes nodes
   DevBuf wnodes;             // traversal copy + flag word
   bool wnodes_valid = false;
+  std::vector<uint32_t> host_off; // host copy of the offsets when they were given on the host
 };
 
 namespace {
@@ -948,6 +954,10 @@ lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const u
   const bool host = !on_device(tris);
   CK(reserve(b->off, 4 * (n_meshes + 1), c->stream), "offset allocation");
   CK(cudaMemcpyAsync(b->off.ptr, offsets, 4 * (n_meshes + 1), cudaMemcpyDefault, c->stream), "offset upload");
+  if (on_device(offsets))
+    b->host_off.clear();
+  else
+    b->host_off.assign(offsets, offsets + n_meshes + 1);
   const void* dt = tris;
   if (host) {
     CK(reserve(b->tris_owned, sizeof(Tri) * total, c->stream), "primitive allocation");
@@ -1012,6 +1022,37 @@ lbvh_batch_nodes(lbvh_ctx* c, const lbvh_batch* b, void* dst)
     return st;
   const bool host = !on_device(dst);
   CK(cudaMemcpyAsync(dst, b->nodes.ptr, sizeof(Node) * (b->total - b->n_meshes), cudaMemcpyDefault, c->stream),
+     "node copy");
+  return host ? check_device(c) : LBVH_OK;
+}
+
+int
+lbvh_batch_mesh_nodes(lbvh_ctx* c, const lbvh_batch* b, size_t k, void* dst)
+{
+  if (!c || !b || !dst)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (!b->n_meshes)
+    return fail(c, LBVH_ERR_INVALID_ARG, "batch has not been built");
+  if (k >= b->n_meshes)
+    return fail(c, LBVH_ERR_INVALID_ARG, "mesh %zu of %u", k, b->n_meshes);
+  int st = set_device(c);
+  if (st)
+    return st;
+  uint32_t o[2];
+  if (!b->host_off.empty()) {
+    o[0] = b->host_off[k];
+    o[1] = b->host_off[k + 1];
+  } else { // offsets were given on the device: read the two that matter
+    CK(cudaMemcpyAsync(c->h_err + 1, static_cast<const uint32_t*>(b->off.ptr) + k, 8, cudaMemcpyDeviceToHost,
+                       c->stream),
+       "offset read");
+    CK(cudaStreamSynchronize(c->stream), "stream synchronize");
+    o[0] = c->h_err[1];
+    o[1] = c->h_err[2];
+  }
+  const bool host = !on_device(dst);
+  CK(cudaMemcpyAsync(dst, static_cast<const Node*>(b->nodes.ptr) + (o[0] - k), sizeof(Node) * (o[1] - o[0] - 1),
+                     cudaMemcpyDefault, c->stream),
      "node copy");
   return host ? check_device(c) : LBVH_OK;
 }
