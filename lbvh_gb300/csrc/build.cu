@@ -427,7 +427,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
 // Global phase (k_tree_global), one thread per pending node, launched after
 // the local phase so that CTAs are not held by the long global chains: the
 // same walk over the global epoch-tagged slots. Every record a thread writes
-// is published with a device-scope fence before its next global arrival.
+// is published by the release half of its next global arrival (an acq_rel exchange).
 
 struct PendingNode
 {
@@ -603,17 +603,16 @@ k_tree_global(Leaf leaf,
   uint32_t L = pn.L, R = pn.R;
   Box box = pn.box;
   const unsigned long long tag = (unsigned long long)epoch << 32;
-  bool wrote = false; // records from the local phase are visible at launch
+  // records from the local phase are visible at launch; a record this thread
+  // writes is published by the release half of its next arrival
+  bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
   for (uint32_t depth = 0;; depth++) {
     if (depth > kMaxTreeDepth + 2) {
       atomicOr(&st->error, kErrBadTopology);
       return;
     }
-    const bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
     const uint32_t s = is_left ? R : L - 1;
-    if (wrote)
-      __threadfence(); // publish this node's record before the sibling can see the slot
-    const unsigned long long old = atomicExch(slots + s, tag | (is_left ? L : R));
+    const unsigned long long old = arrive_acq_rel(slots + s, tag | (is_left ? L : R));
     if (uint32_t(old >> 32) != epoch)
       return; // first arrival: the sibling completes the parent
     const uint32_t far = uint32_t(old);
@@ -622,12 +621,10 @@ k_tree_global(Leaf leaf,
     const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
     const uint32_t sib = is_left ? cr : cl;
     Box other;
-    if (sib & kLeafBit) {
+    if (sib & kLeafBit)
       other = leaf(sib & ~kLeafBit);
-    } else {
-      __threadfence(); // the sibling's record was published before its swap
-      other = load_node_box(nodes, sib);
-    }
+    else
+      other = load_node_box(nodes, sib); // published before the sibling's swap, seen after ours
     box = is_left ? join(box, other) : join(other, box);
     L = LP;
     R = RP;
@@ -635,9 +632,8 @@ k_tree_global(Leaf leaf,
       store_node(nodes, 0, box, cl, cr);
       return;
     }
-    const bool up_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
-    store_node(nodes, up_left ? R : L, box, cl, cr);
-    wrote = true;
+    is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+    store_node(nodes, is_left ? R : L, box, cl, cr);
   }
 }
 
@@ -740,9 +736,9 @@ k_refit(Leaf leaf,
       atomicOr(&st->error, kErrBadTopology);
       return;
     }
-    if (!(self & kLeafBit))
-      __threadfence(); // publish this node's record before arriving
-    const unsigned long long old = atomicExch(slots + q, tag);
+    // release: this thread's last record is published; acquire: the
+    // sibling's record, published by its own arrival, is visible below
+    const unsigned long long old = arrive_acq_rel(slots + q, tag);
     if (uint32_t(old >> 32) != epoch)
       return;
     const uint2 lr = __ldg(child + q);
@@ -753,12 +749,10 @@ k_refit(Leaf leaf,
     }
     const uint32_t sib = (lr.x == self) ? lr.y : lr.x;
     Box other;
-    if (sib & kLeafBit) {
+    if (sib & kLeafBit)
       other = leaf(sib & ~kLeafBit);
-    } else {
-      __threadfence();
+    else
       other = load_node_box(nodes, sib);
-    }
     box = (lr.x == self) ? join(box, other) : join(other, box);
     store_node(nodes, q, box, lr.x, lr.y);
     if (q == 0)

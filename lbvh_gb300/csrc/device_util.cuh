@@ -120,6 +120,19 @@ store_node(Node* __restrict__ nodes, uint32_t idx, const Box& b, uint32_t l, uin
   __stcg(dst + 1, make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r)));
 }
 
+// Arrival at a device-scope slot: swaps in `v` and returns the previous word,
+// with release semantics (this thread's earlier stores, e.g. the record of the
+// node it just finished, become visible to whoever reads `v`) and acquire
+// semantics (the stores that the previous writer made before its own swap,
+// e.g. the sibling's record, are visible to this thread's later loads).
+__device__ __forceinline__ unsigned long long
+arrive_acq_rel(unsigned long long* slot, unsigned long long v)
+{
+  unsigned long long old;
+  asm volatile("atom.acq_rel.gpu.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(slot), "l"(v) : "memory");
+  return old;
+}
+
 __device__ __forceinline__ Box
 load_node_box(const Node* __restrict__ nodes, uint32_t idx)
 {
