@@ -414,7 +414,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
 // Local phase (k_tree_local), one CTA per kTreeBlock consecutive leaf slots:
 // every node whose range lies inside the CTA's slots finds its parent's
 // arrival slot and its sibling's record in shared memory, and threads walk up
-// with shared-memory atomics and block-scope fences only. Lanes take leaf
+// with block-scope acquire-release exchanges on shared memory only. Lanes take leaf
 // slots from a CTA queue (one shared atomic per warp refill), so a lane whose
 // walk ended starts the next one instead of idling while its warp finishes.
 // A walk ends at a first arrival, or at a node whose parent's split lies on
@@ -512,14 +512,14 @@ k_tree_local(Leaf leaf,
       active = false;
       continue;
     }
-    __threadfence_block();
-    const uint32_t old = atomicExch(s_slot + (s - b0), is_left ? L : R);
+    // release publishes this thread's staged record, acquire makes the
+    // sibling's visible
+    const uint32_t old = arrive_acq_rel_cta(s_slot + (s - b0), is_left ? L : R);
     if (old == kSlotEmpty) {
       active = false; // first arrival: recoverable from the slot if unmatched
       continue;
     }
-    s_slot[s - b0] = kSlotComplete;
-    __threadfence_block();
+    s_slot[s - b0] = kSlotComplete; // read only after the block barrier below
     const uint32_t LP = is_left ? L : old, RP = is_left ? old : R;
     const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
     const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);

@@ -133,6 +133,16 @@ arrive_acq_rel(unsigned long long* slot, unsigned long long v)
   return old;
 }
 
+// The same arrival on a shared-memory slot, ordered at block scope.
+__device__ __forceinline__ uint32_t
+arrive_acq_rel_cta(uint32_t* slot, uint32_t v)
+{
+  uint32_t old;
+  const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(slot));
+  asm volatile("atom.acq_rel.cta.shared::cta.exch.b32 %0, [%1], %2;" : "=r"(old) : "r"(addr), "r"(v) : "memory");
+  return old;
+}
+
 __device__ __forceinline__ Box
 load_node_box(const Node* __restrict__ nodes, uint32_t idx)
 {
