@@ -184,6 +184,31 @@ LBVH_API int lbvh_bvh_curve(lbvh_ctx* ctx, const lbvh_bvh* bvh, uint32_t* codes,
  * 2055-2075) for m rays: rays is m x 8 float32, hits receives m lbvh_hit.
  * Requires a BVH built from triangles. */
 LBVH_API int lbvh_trace_triangles(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* rays, size_t m, void* hits);
+/* The sphere primitive and hit of the reference's example program
+ * (examples/minimal.cpp:16-42): a sphere is {radius, x, y, z}; a hit is
+ * sphere_hit {tmin, uv, normal} with the hit sphere's index. A miss is
+ * {LBVH_MISS, +inf, 0, 0, {0, 0, 0}}. */
+typedef struct lbvh_sphere_hit
+{
+  uint32_t prim;
+  float t;
+  float u;
+  float v;
+  float normal[3];
+  float pad;
+} lbvh_sphere_hit;
+
+/* Replaces traverser<float, sphere, sphere_hit>::operator()(ray,
+ * intersect_sphere) (lbvh.h:1869-1942 with the intersector of
+ * examples/minimal.cpp:92-135) for m rays: the user-primitive path, the
+ * intersector running on the device. `bvh` must have been built, without
+ * LBVH_BUILD_SORTED_LEAVES, from these n spheres' boxes (the example's
+ * sphere_to_box: {pos - radius, pos + radius}, e.g. with lbvh_build_boxes).
+ * spheres is n x 4 float32, rays m x 8 float32, hits m lbvh_sphere_hit. The
+ * hit index, t and normal are bit-identical to the reference; u and v come
+ * from atan2 and acos and agree to within a few units in the last place. */
+LBVH_API int lbvh_trace_spheres(lbvh_ctx* ctx, const lbvh_bvh* bvh, const float* spheres, const float* rays, size_t m,
+                                void* hits);
 /* Makes the BVH's traversal copy now, on the context's stream (traces make
  * it on first use otherwise). Callers that trace one BVH from several streams
  * call this once after each build / refit / import, before those traces. */

@@ -12,12 +12,15 @@ from .api import (  # noqa: F401
     LEAF_BIT,
     MISS,
     NODE_DTYPE,
+    SPHERE_HIT_DTYPE,
     TRIANGLES,
     Builder,
     Context,
     LbvhError,
+    SphereTraverser,
     Traverser,
     default_context,
     hits_view,
     make_triangles,
+    sphere_boxes,
 )

@@ -62,6 +62,7 @@ SIGNATURES = {
     "lbvh_bvh_device_nodes": (_P, [_P]),
     "lbvh_bvh_curve": (_I, [_P, _P, _P, _P, _P, _P]),
     "lbvh_trace_triangles": (_I, [_P, _P, _P, _S, _P]),
+    "lbvh_trace_spheres": (_I, [_P, _P, _P, _P, _S, _P]),
     "lbvh_trace_triangles_counts": (_I, [_P, _P, _P, _S, _P, _P, _P]),
     "lbvh_build_triangles_noalloc": (_I, [_P, _S, _P, _P, _P]),
     "lbvh_bvh_prepare_trace": (_I, [_P, _P]),

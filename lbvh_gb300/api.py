@@ -33,6 +33,11 @@ NODE_DTYPE = np.dtype(
     [("lo", "<f4", (3,)), ("hi", "<f4", (3,)), ("left", "<u4"), ("right", "<u4")]
 )
 HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+# lbvh_sphere_hit: the example program's sphere_hit {tmin, uv, normal} with
+# the hit sphere's index (examples/minimal.cpp:24-42)
+SPHERE_HIT_DTYPE = np.dtype(
+    [("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("normal", "<f4", (3,)), ("pad", "<f4")]
+)
 LEAF_BIT = _lib.LEAF_BIT
 MISS = _lib.MISS
 
@@ -348,6 +353,44 @@ class Traverser:
                                                          _addr(out), _addr(nb), _addr(nt)))
             return out, nb, nt
         self.ctx.check(L.lbvh_trace_triangles(self.ctx.handle, self.bvh.handle, _addr(rays), m, _addr(out)))
+        return out
+
+
+def sphere_boxes(spheres) -> np.ndarray:
+    """The example program's sphere_to_box converter (examples/minimal.cpp:
+    62-67) for {radius, x, y, z} rows: {pos - radius, pos + radius}, float32.
+    It runs on the host, as the reference runs a caller's converter; build
+    with Builder()(boxes, converter=BOXES)."""
+    s = np.ascontiguousarray(spheres, dtype=np.float32).reshape(-1, 4)
+    r = s[:, :1]
+    return np.ascontiguousarray(np.concatenate([s[:, 1:] - r, s[:, 1:] + r], axis=1), dtype=np.float32)
+
+
+class SphereTraverser:
+    """traverser<float, sphere, sphere_hit> with the example program's
+    intersector, run on the device (lbvh_trace_spheres): the user-primitive
+    path. `bvh` is built from sphere_boxes(spheres) in reference leaf order;
+    hit index, t and normal are bit-identical to the reference, u and v agree
+    to within a few units in the last place (atan2 / acos)."""
+
+    def __init__(self, bvh: BVH, spheres):
+        if bvh.info()[2] & _lib.LBVH_BUILD_SORTED_LEAVES:
+            raise ValueError("sphere traces need a BVH in reference leaf order")
+        self.bvh = bvh
+        self.ctx = bvh.ctx
+        self.spheres = spheres if _is_cuda(spheres) else np.ascontiguousarray(spheres, dtype=np.float32)
+        if _rows(self.spheres, 4, "spheres") != len(bvh) + 1:
+            raise ValueError("need one sphere per leaf")
+
+    def __call__(self, rays, out=None):
+        m = _rows(rays, 8, "rays")
+        if out is None:
+            if _is_cuda(rays):
+                out = torch.empty((m, 8), dtype=torch.float32, device=rays.device)
+            else:
+                out = np.empty(m, SPHERE_HIT_DTYPE)
+        self.ctx.check(_lib.lib().lbvh_trace_spheres(self.ctx.handle, self.bvh.handle, _addr(self.spheres),
+                                                     _addr(rays), m, _addr(out)))
         return out
 
 

@@ -830,6 +830,57 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
 }
 
 int
+lbvh_trace_spheres(lbvh_ctx* c, const lbvh_bvh* b, const float* spheres, const float* rays, size_t m, void* hits)
+{
+  if (!c || !b || !spheres || (m && (!rays || !hits)))
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (b->n < 2)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH has not been built");
+  if (b->flags & LBVH_BUILD_SORTED_LEAVES)
+    return fail(c, LBVH_ERR_INVALID_ARG, "sphere traces need reference leaf order (a build without sorted leaves)");
+  if (m > 0x7fffffffull)
+    return fail(c, LBVH_ERR_INVALID_ARG, "ray count %zu too large", m);
+  if (m == 0)
+    return LBVH_OK;
+  int st = set_device(c);
+  if (st)
+    return st;
+  const size_t n = b->n;
+  const bool hs = !on_device(spheres), hr = !on_device(rays), hh = !on_device(hits);
+  const float* ds = spheres;
+  const float* dr = rays;
+  SphereHit* dh = static_cast<SphereHit*>(hits);
+  if (hs) {
+    CK(reserve(c->prims_in, 16 * n, c->stream), "sphere staging allocation");
+    CK(cudaMemcpyAsync(c->prims_in.ptr, spheres, 16 * n, cudaMemcpyHostToDevice, c->stream), "sphere upload");
+    ds = static_cast<const float*>(c->prims_in.ptr);
+  } else if (reinterpret_cast<uintptr_t>(spheres) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device spheres must be 16-byte aligned");
+  }
+  if (hr) {
+    CK(reserve(c->rays, 32 * m, c->stream), "ray staging allocation");
+    CK(cudaMemcpyAsync(c->rays.ptr, rays, 32 * m, cudaMemcpyHostToDevice, c->stream), "ray upload");
+    dr = static_cast<const float*>(c->rays.ptr);
+  } else if (reinterpret_cast<uintptr_t>(rays) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device rays must be 16-byte aligned");
+  }
+  if (hh) {
+    CK(reserve(c->hits, sizeof(SphereHit) * m, c->stream), "hit staging allocation");
+    dh = static_cast<SphereHit*>(c->hits.ptr);
+  } else if (reinterpret_cast<uintptr_t>(hits) & 15) {
+    return fail(c, LBVH_ERR_INVALID_ARG, "device hits must be 16-byte aligned");
+  }
+  if ((st = ensure_wnodes(c, const_cast<lbvh_bvh*>(b))))
+    return st;
+  CK(launch_trace_spheres(static_cast<const WideNode*>(b->wnodes.ptr), reinterpret_cast<const float4*>(ds), dr,
+                          uint32_t(m), dh, c->num_sms, c->stream),
+     "sphere trace launch");
+  if (hh)
+    CK(cudaMemcpyAsync(hits, dh, sizeof(SphereHit) * m, cudaMemcpyDeviceToHost, c->stream), "hit download");
+  return (hs || hr || hh) ? check_device(c) : LBVH_OK;
+}
+
+int
 lbvh_trace_triangles(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* hits)
 {
   return trace_common(c, b, rays, m, hits, nullptr, nullptr);

@@ -392,6 +392,141 @@ launch_trace_tris(const WideNode* wnodes,
 }
 
 // ---------------------------------------------------------------------------
+// User-primitive traversal: spheres with the intersector of the reference's
+// example program (examples/minimal.cpp:92-135), over a tree built from the
+// spheres' boxes. The traversal is traverser::operator() (lbvh.h:1874-1942)
+// with the intersector swapped: one thread per ray, the same visiting order,
+// stack semantics and closest-hit rule (a result replaces the closest only
+// when its t is smaller; leaf children are tested left first).
+
+struct SphereInfo
+{
+  float t, u, v, nx, ny, nz;
+};
+
+// The example's sphere intersection, with its operation order: the nearer
+// root unless it is negative (then the other root, negative or not), the
+// normal normalized as lbvh::math::normalize does (lbvh.h:724-734), and uv
+// from atan2 / acos. A ray that misses returns t = +inf. The ray's tmin and
+// tmax are not consulted, as in the example.
+__device__ __forceinline__ SphereInfo
+sphere_test(const RayCtx& r, float4 s)
+{
+  const float inf = __int_as_float(0x7f800000);
+  const float rad = s.x, cx = s.y, cy = s.z, cz = s.w;
+  const float ox = fsub(r.px, cx), oy = fsub(r.py, cy), oz = fsub(r.pz, cz); // ray.pos - s_pos
+  const float a = dot3(r.dx, r.dy, r.dz, r.dx, r.dy, r.dz);
+  const float b = fmul(2.0f, dot3(r.dx, r.dy, r.dz, ox, oy, oz));
+  const float c = fsub(dot3(ox, oy, oz, ox, oy, oz), fmul(rad, rad));
+  const float disc = fsub(fmul(b, b), fmul(fmul(4.0f, a), c));
+  if (disc < 0.0f)
+    return SphereInfo{ inf, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f };
+  const float sq = __fsqrt_rn(disc);
+  const float den = fmul(2.0f, a);
+  const float t0 = fdiv(fadd(-b, sq), den);
+  const float t1 = fdiv(fsub(-b, sq), den);
+  const float t = (t0 < 0.0f) ? t1 : t0;
+  const float vx = fsub(fadd(r.px, fmul(r.dx, t)), cx); // hit_pos - s_pos
+  const float vy = fsub(fadd(r.py, fmul(r.dy, t)), cy);
+  const float vz = fsub(fadd(r.pz, fmul(r.dz, t)), cz);
+  const float l_inv = fdiv(1.0f, __fsqrt_rn(dot3(vx, vy, vz, vx, vy, vz)));
+  const float nx = fmul(vx, l_inv), ny = fmul(vy, l_inv), nz = fmul(vz, l_inv);
+  const float pi = 3.14159274101257324f; // float(M_PI)
+  return SphereInfo{ t, fmul(fadd(1.0f, fdiv(atan2f(nz, nx), pi)), 0.5f), fdiv(acosf(ny), pi), nx, ny, nz };
+}
+
+__global__ __launch_bounds__(kTraceThreads) void
+k_trace_spheres(const WideNode* __restrict__ wnodes,
+                const float4* __restrict__ spheres,
+                const float4* __restrict__ rays,
+                uint32_t m,
+                SphereHit* __restrict__ hits)
+{
+  const float inf = __int_as_float(0x7f800000);
+  uint2 stack[kStackSize];
+  for (uint32_t ray = blockIdx.x * blockDim.x + threadIdx.x; ray < m; ray += gridDim.x * blockDim.x) {
+    RayCtx r = make_ray(__ldg(rays + 2 * size_t(ray)), __ldg(rays + 2 * size_t(ray) + 1));
+    r.fast = false; // the reference's own min/max ternaries throughout
+    uint32_t best_p = kMiss;
+    SphereInfo best{ inf, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f };
+    uint32_t sp = 0;
+    stack[sp++] = make_uint2(0u, __float_as_uint(inf)); // root, pushed with +inf
+    while (sp) {
+      const uint2 e = stack[--sp];
+      if (best.t < __uint_as_float(e.y))
+        continue;
+      const float4* w = reinterpret_cast<const float4*>(wnodes + e.x);
+      const float4 A = __ldg(w + 0), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+      const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
+      bool lhit = false, rhit = false;
+      float lt = inf, rt = inf;
+      if (left & kLeafBit) {
+        const uint32_t p = left & ~kLeafBit;
+        const SphereInfo h = sphere_test(r, __ldg(spheres + p));
+        if (h.t < best.t) {
+          best = h;
+          best_p = p;
+        }
+      } else {
+        lhit = box_test(r, A.x, A.y, A.z, A.w, B.x, B.y, lt);
+      }
+      if (right & kLeafBit) {
+        const uint32_t p = right & ~kLeafBit;
+        const SphereInfo h = sphere_test(r, __ldg(spheres + p));
+        if (h.t < best.t) {
+          best = h;
+          best_p = p;
+        }
+      } else {
+        rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
+      }
+      if (lhit && rhit) {
+        const bool lfirst = lt < rt; // left nearer: push right, then left
+        const uint2 far = lfirst ? make_uint2(right, __float_as_uint(rt)) : make_uint2(left, __float_as_uint(lt));
+        const uint2 near = lfirst ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
+        if (sp < kStackSize)
+          stack[sp++] = far;
+        if (sp < kStackSize)
+          stack[sp++] = near;
+      } else if (lhit || rhit) {
+        if (sp < kStackSize)
+          stack[sp++] = lhit ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
+      }
+    }
+    SphereHit out;
+    out.prim = best_p;
+    if (best_p == kMiss)
+      best = SphereInfo{ inf, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f };
+    out.t = best.t;
+    out.u = best.u;
+    out.v = best.v;
+    out.nx = best.nx;
+    out.ny = best.ny;
+    out.nz = best.nz;
+    out.pad = 0.0f;
+    hits[ray] = out;
+  }
+}
+
+cudaError_t
+launch_trace_spheres(const WideNode* wnodes,
+                     const float4* spheres,
+                     const float* rays,
+                     uint32_t m,
+                     SphereHit* hits,
+                     int num_sms,
+                     cudaStream_t s)
+{
+  if (m == 0)
+    return cudaSuccess;
+  const uint32_t want = ceil_div_u32(m, kTraceThreads);
+  const uint32_t cap = uint32_t(num_sms) * 8;
+  k_trace_spheres<<<want < cap ? want : cap, kTraceThreads, 0, s>>>(wnodes, spheres,
+                                                                   reinterpret_cast<const float4*>(rays), m, hits);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // batched meshes (launch_batch_repack / launch_batch_trace, batch.cuh)
 
 __global__ void

@@ -42,4 +42,21 @@ cudaError_t launch_trace_tris(const WideNode* wnodes,
                               const TraceParams& p,
                               cudaStream_t s);
 
+// Hit record of the sphere intersector: {prim, t, uv, normal, pad}, 32 bytes.
+struct __align__(16) SphereHit
+{
+  uint32_t prim;
+  float t, u, v;
+  float nx, ny, nz, pad;
+};
+
+// spheres: n x {radius, x, y, z}; leaf slot p is sphere p (parity leaf order).
+cudaError_t launch_trace_spheres(const WideNode* wnodes,
+                                 const float4* spheres,
+                                 const float* rays,
+                                 uint32_t m,
+                                 SphereHit* hits,
+                                 int num_sms,
+                                 cudaStream_t s);
+
 } // namespace lbvh_gb300

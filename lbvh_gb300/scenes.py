@@ -439,3 +439,40 @@ def served_requests(n_requests: int, rate: float, seed: int, n_scenes: int = 48,
         else:
             out.append((float(t[i]), "build", s, meshes[s]))
     return out
+
+
+def example_spheres() -> np.ndarray:
+    """The three spheres of the reference's example program
+    (examples/minimal.cpp:48-50), as {radius, x, y, z} rows."""
+    return np.array([[1, 5, 1, -5], [1, 0, 2, -5], [1, -5, 1, -5]], np.float32)
+
+
+def example_camera_rays(width: int, height: int) -> np.ndarray:
+    """The example program's camera (examples/minimal.cpp:140-160) at a
+    chosen resolution: origin (0, 0, 5), direction {x_ndc * aspect * 0.75,
+    y_ndc * 0.75, -1} through pixel centres, row-major from the top; tmin = 0,
+    tmax = +inf. Computed in float32."""
+    f32 = np.float32
+    x = (np.arange(width, dtype=f32) + f32(0.5))
+    y = (np.arange(height, dtype=f32) + f32(0.5))
+    x_ndc = (f32(2) * x / f32(width)) - f32(1)
+    y_ndc = -(f32(2) * y / f32(height)) + f32(1)
+    aspect = f32(width) / f32(height)
+    fov = f32(0.75)
+    out = np.zeros((height, width, 8), f32)
+    out[..., 2] = 5
+    out[..., 3] = (x_ndc * aspect * fov)[None, :]
+    out[..., 4] = (y_ndc * fov)[:, None]
+    out[..., 5] = -1
+    out[..., 7] = np.inf
+    return out.reshape(-1, 8)
+
+
+def sphere_scene(n: int, seed: int, extent: float = 6.0, r_lo: float = 0.02, r_hi: float = 0.3) -> np.ndarray:
+    """n spheres {radius, x, y, z}: centres uniform in a cube of side
+    `extent` about the origin, radii uniform in [r_lo, r_hi]."""
+    u = uniform(seed, 80, 4 * n).reshape(n, 4)
+    out = np.empty((n, 4), np.float32)
+    out[:, 0] = r_lo + (r_hi - r_lo) * u[:, 0]
+    out[:, 1:] = (u[:, 1:] - 0.5) * extent
+    return out

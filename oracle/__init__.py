@@ -33,6 +33,9 @@ NODE_DTYPE = np.dtype(
     [("lo", "<f4", (3,)), ("hi", "<f4", (3,)), ("left", "<u4"), ("right", "<u4")]
 )
 HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+SPHERE_HIT_DTYPE = np.dtype(
+    [("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("normal", "<f4", (3,)), ("pad", "<f4")]
+)
 LEAF_BIT = 0x80000000
 MISS = 0xFFFFFFFF
 
@@ -132,6 +135,7 @@ class Port(_Lib):
         f("refit", ctypes.c_int, [_P, _S, _P])
         f("trace", None, [_P, _P, _P, _S, _S, _P, _P, _P])
         f("check_bvh", ctypes.c_long, [_P, _S])
+        f("trace_spheres", None, [_P, _P, _P, _S, _S, _P])
 
     def split(self, sorted_codes: np.ndarray) -> np.ndarray:
         c = np.ascontiguousarray(sorted_codes, dtype=np.uint32)
@@ -157,6 +161,16 @@ class Port(_Lib):
         self._trace(_ptr(nd), _ptr(t), _ptr(r), m, threads, _ptr(hits), _ptr(nb), _ptr(nt))
         return (hits, nb, nt) if counts else hits
 
+    def trace_spheres(self, nodes, spheres, rays, threads: int = 1):
+        """Closest sphere hits (the example program's intersector) over a
+        tree built from the spheres' boxes."""
+        nd = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        sp = np.ascontiguousarray(spheres, dtype=np.float32).reshape(-1, 4)
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        hits = np.empty(r.shape[0], SPHERE_HIT_DTYPE)
+        self._trace_spheres(_ptr(nd), _ptr(sp), _ptr(r), r.shape[0], threads, _ptr(hits))
+        return hits
+
     def check_bvh(self, nodes) -> int:
         nd = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
         return int(self._check_bvh(_ptr(nd), nd.size))
@@ -170,6 +184,7 @@ class Ref(_Lib):
         f = self._f
         f("trace", None, [_P, _S, _P, _S, _P, _S, _S, _P])
         f("load_obj", ctypes.c_long, [ctypes.c_char_p, _P, _S])
+        f("trace_spheres", None, [_P, _S, _P, _S, _P, _S, _S, _P])
 
     def trace(self, nodes, tris, rays, threads: int = 1):
         nd = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
@@ -178,6 +193,14 @@ class Ref(_Lib):
         m = r.shape[0]
         hits = np.empty(m, HIT_DTYPE)
         self._trace(_ptr(nd), nd.size, _ptr(t), t.shape[0], _ptr(r), m, threads, _ptr(hits))
+        return hits
+
+    def trace_spheres(self, nodes, spheres, rays, threads: int = 1):
+        nd = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        sp = np.ascontiguousarray(spheres, dtype=np.float32).reshape(-1, 4)
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        hits = np.empty(r.shape[0], SPHERE_HIT_DTYPE)
+        self._trace_spheres(_ptr(nd), nd.size, _ptr(sp), sp.shape[0], _ptr(r), r.shape[0], threads, _ptr(hits))
         return hits
 
     def load_obj(self, path: str) -> np.ndarray:

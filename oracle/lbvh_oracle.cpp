@@ -488,6 +488,132 @@ trace_one(const node32* nodes,
 
 } // namespace
 
+// ---------------------------------------------------------------------------
+// User primitive: the sphere of the reference's example program
+// (examples/minimal.cpp:16-42, {radius, pos}) with its intersector
+// (examples/minimal.cpp:92-135), traced by traverser::operator()
+// (lbvh.h:1874-1942) with that intersector swapped in.
+
+struct sphere16
+{
+  float radius;
+  float pos[3];
+};
+static_assert(sizeof(sphere16) == 16, "sphere layout is 16 bytes");
+
+struct sphere_hit32
+{
+  uint32_t prim;
+  float t, u, v;
+  float n[3];
+  float pad;
+};
+static_assert(sizeof(sphere_hit32) == 32, "sphere hit layout is 32 bytes");
+
+// normalize, lbvh.h:724-734: v * (1 / sqrt(dot(v, v)))
+inline v3
+normalize(v3 v)
+{
+  const float l_inv = 1.0f / std::sqrt(dot(v, v));
+  return v3{ v.x * l_inv, v.y * l_inv, v.z * l_inv };
+}
+
+// The example's intersector: t = +inf when the ray's line misses; otherwise
+// the root (-b + sqrt(disc)) / 2a unless it is negative, then the other one.
+inline sphere_hit32
+sphere_hit(const sphere16& s, v3 pos, v3 dir)
+{
+  sphere_hit32 h{ 0xffffffffu, kInf, 0.0f, 0.0f, { 0.0f, 0.0f, 0.0f }, 0.0f };
+  const v3 sp{ s.pos[0], s.pos[1], s.pos[2] };
+  const v3 dist = vsub(pos, sp);
+  const float a = dot(dir, dir);
+  const float b = 2 * dot(dir, dist);
+  const float c = dot(dist, dist) - (s.radius * s.radius);
+  const float disc = (b * b) - (4 * a * c);
+  if (disc < 0)
+    return h;
+  const float t0 = (-b + std::sqrt(disc)) / (2 * a);
+  const float t1 = (-b - std::sqrt(disc)) / (2 * a);
+  float t = t0;
+  if (t < 0)
+    t = t1;
+  const v3 hit{ pos.x + (dir.x * t), pos.y + (dir.y * t), pos.z + (dir.z * t) };
+  const v3 n = normalize(vsub(hit, sp));
+  const float pi = float(M_PI);
+  h.t = t;
+  h.u = (1.0f + std::atan2(n.z, n.x) / pi) * 0.5f;
+  h.v = std::acos(n.y) / pi;
+  h.n[0] = n.x;
+  h.n[1] = n.y;
+  h.n[2] = n.z;
+  return h;
+}
+
+inline sphere_hit32
+trace_sphere_one(const node32* nodes, const sphere16* spheres, const float* ray)
+{
+  struct ent
+  {
+    uint32_t node;
+    float tmin;
+  };
+  ent stack[128];
+  size_t sp = 0;
+  stack[sp++] = ent{ 0, kInf };
+  const v3 pos{ ray[0], ray[1], ray[2] };
+  const v3 dir{ ray[3], ray[4], ray[5] };
+  const accel a = make_accel(pos, dir);
+  sphere_hit32 best{ 0xffffffffu, kInf, 0.0f, 0.0f, { 0.0f, 0.0f, 0.0f }, 0.0f };
+  while (sp) {
+    const ent e = stack[--sp];
+    if (best.t < e.tmin)
+      continue;
+    const node32& nd = nodes[e.node];
+    bool lhit = false, rhit = false;
+    float lt = kInf, rt = kInf;
+    if (nd.left & kLeafBit) {
+      const uint32_t p = nd.left & ~kLeafBit;
+      sphere_hit32 h = sphere_hit(spheres[p], pos, dir);
+      if (h.t < best.t) {
+        h.prim = p;
+        best = h;
+      }
+    } else {
+      lhit = box_hit(nodes[nd.left].box, a, lt);
+    }
+    if (nd.right & kLeafBit) {
+      const uint32_t p = nd.right & ~kLeafBit;
+      sphere_hit32 h = sphere_hit(spheres[p], pos, dir);
+      if (h.t < best.t) {
+        h.prim = p;
+        best = h;
+      }
+    } else {
+      rhit = box_hit(nodes[nd.right].box, a, rt);
+    }
+    if (lhit && rhit) {
+      if (lt < rt) {
+        if (sp < 128)
+          stack[sp++] = ent{ nd.right, rt };
+        if (sp < 128)
+          stack[sp++] = ent{ nd.left, lt };
+      } else {
+        if (sp < 128)
+          stack[sp++] = ent{ nd.left, lt };
+        if (sp < 128)
+          stack[sp++] = ent{ nd.right, rt };
+      }
+    } else if (lhit) {
+      if (sp < 128)
+        stack[sp++] = ent{ nd.left, lt };
+    } else if (rhit) {
+      if (sp < 128)
+        stack[sp++] = ent{ nd.right, rt };
+    }
+  }
+  return best;
+}
+
 extern "C" {
 
 // triangle<float>(a, b, c), lbvh.h:1967-1972: e0 = a - b, e1 = c - a,
@@ -618,6 +744,21 @@ orc_trace(const void* nodes,
   run_threads(threads, [&](size_t idx, size_t cnt) {
     for (size_t i = idx; i < m; i += cnt)
       h[i] = trace_one(nd, t, rays + 8 * i, n_box ? n_box + i : nullptr, n_tri ? n_tri + i : nullptr);
+  });
+}
+
+// Closest sphere hit of m rays (8 floats) over a tree built from the
+// spheres' boxes; hits are 32 bytes {prim, t, u, v, normal, pad}, misses
+// {UINT32_MAX, +inf, 0, 0, 0, 0, 0}.
+void
+orc_trace_spheres(const void* nodes, const float* spheres, const float* rays, size_t m, size_t threads, void* out_hits)
+{
+  const node32* nd = static_cast<const node32*>(nodes);
+  const sphere16* sph = reinterpret_cast<const sphere16*>(spheres);
+  sphere_hit32* h = static_cast<sphere_hit32*>(out_hits);
+  run_threads(threads, [&](size_t idx, size_t cnt) {
+    for (size_t i = idx; i < m; i += cnt)
+      h[i] = trace_sphere_one(nd, sph, rays + 8 * i);
   });
 }
 

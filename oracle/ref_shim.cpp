@@ -10,6 +10,8 @@
 //   bounds  -> detail::centroid_bounds_kernel + union    (lbvh.h:1282-1293,1532-1543)
 //   sort    -> detail::space_filling_curve::sort         (lbvh.h:1126-1134)
 //   trace   -> lbvh::traverser<...>::operator()          (lbvh.h:1869-1942)
+//   spheres -> the same traverser with the example program's sphere type
+//              and intersector (examples/minimal.cpp:16-42, 92-135), restated
 //   triangle/ctor, converter, intersector                (lbvh.h:1959-2076)
 //   OBJ load -> tinyobj::ObjReader as lbvh_test.cpp:602-649 uses it
 //
@@ -22,8 +24,10 @@
 #include "third-party/tiny_obj_loader.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 namespace {
@@ -52,6 +56,80 @@ struct hit_out
   float u;
   float v;
 };
+
+// The sphere and sphere_hit types of the reference's example program
+// (examples/minimal.cpp:16-42), restated: a sphere is {radius, pos}; a hit
+// orders by tmin, against another hit and against a distance.
+struct sphere_t
+{
+  float radius;
+  float pos[3];
+};
+
+struct sphere_hit_t
+{
+  float tmin = std::numeric_limits<float>::infinity();
+  float uv[2]{ 0, 0 };
+  float normal[3]{ 0, 0, 0 };
+  bool operator<(const sphere_hit_t& other) const noexcept { return tmin < other.tmin; }
+  bool operator<(float distance) const noexcept { return tmin < distance; }
+};
+
+struct sphere_hit_out
+{
+  uint32_t prim;
+  float t, u, v;
+  float n[3];
+  float pad;
+};
+
+// The example's intersector (examples/minimal.cpp:92-135), restated in plain
+// float operations in the example's order (the same order the port and the
+// GPU kernel use): the quadratic's roots, the nearer unless negative, the
+// normal as lbvh::math::normalize forms it, uv from atan2 and acos.
+sphere_hit_t
+intersect_sphere(const sphere_t& s, const lbvh::ray<float>& ray)
+{
+  const float ox = ray.pos.x - s.pos[0], oy = ray.pos.y - s.pos[1], oz = ray.pos.z - s.pos[2];
+  const float dx = ray.dir.x, dy = ray.dir.y, dz = ray.dir.z;
+  float dd = 0, dof = 0, oo = 0; // dot products accumulate from 0 in x, y, z order
+  dd += dx * dx;
+  dd += dy * dy;
+  dd += dz * dz;
+  dof += dx * ox;
+  dof += dy * oy;
+  dof += dz * oz;
+  oo += ox * ox;
+  oo += oy * oy;
+  oo += oz * oz;
+  const float qb = 2.0f * dof;
+  const float qc = oo - s.radius * s.radius;
+  const float disc = qb * qb - (4.0f * dd) * qc;
+  sphere_hit_t h;
+  if (disc < 0)
+    return h;
+  const float root = std::sqrt(disc);
+  const float near = (-qb + root) / (2.0f * dd);
+  const float other = (-qb - root) / (2.0f * dd);
+  const float t = near < 0 ? other : near;
+  const float vx = (ray.pos.x + dx * t) - s.pos[0];
+  const float vy = (ray.pos.y + dy * t) - s.pos[1];
+  const float vz = (ray.pos.z + dz * t) - s.pos[2];
+  float vv = 0;
+  vv += vx * vx;
+  vv += vy * vy;
+  vv += vz * vz;
+  const float inv_len = 1.0f / std::sqrt(vv);
+  const float nx = vx * inv_len, ny = vy * inv_len, nz = vz * inv_len;
+  const float pi = float(M_PI);
+  h.tmin = t;
+  h.uv[0] = (1.0f + std::atan2(nz, nx) / pi) * 0.5f;
+  h.uv[1] = std::acos(ny) / pi;
+  h.normal[0] = nx;
+  h.normal[1] = ny;
+  h.normal[2] = nz;
+  return h;
+}
 
 } // namespace
 
@@ -200,6 +278,45 @@ ref_trace(const void* nodes,
                            std::numeric_limits<float>::infinity(),
                            0.0f,
                            0.0f };
+    }
+  };
+  lbvh::naive_thread_scheduler sched(threads);
+  sched(work);
+}
+
+// traverser<float, sphere, sphere_hit>::operator() with the example's
+// intersector over a node array built from the spheres' boxes.
+void
+ref_trace_spheres(const void* nodes,
+                  size_t n_nodes,
+                  const float* spheres,
+                  size_t n_spheres,
+                  const float* rays,
+                  size_t m,
+                  size_t threads,
+                  void* out_hits)
+{
+  std::vector<node_t> nv(n_nodes);
+  std::memcpy(nv.data(), nodes, n_nodes * sizeof(node_t));
+  lbvh::bvh<float> bvh(std::move(nv));
+  std::vector<sphere_t> sv(n_spheres);
+  std::memcpy(sv.data(), spheres, n_spheres * sizeof(sphere_t));
+  lbvh::traverser<float, sphere_t, sphere_hit_t> trav(bvh, sv.data());
+  auto* hits = static_cast<sphere_hit_out*>(out_hits);
+  auto work = [&](lbvh::work_division div) {
+    for (size_t i = div.idx; i < m; i += div.max) {
+      const float* r = rays + i * 8;
+      lbvh::ray<float> ray{ { r[0], r[1], r[2] }, { r[3], r[4], r[5] }, r[6], r[7] };
+      auto isect = trav(ray, intersect_sphere);
+      sphere_hit_out o{ 0xffffffffu, std::numeric_limits<float>::infinity(), 0.0f, 0.0f, { 0, 0, 0 }, 0.0f };
+      if (isect)
+        o = sphere_hit_out{ isect.primitive,
+                            isect.info.tmin,
+                            isect.info.uv[0],
+                            isect.info.uv[1],
+                            { isect.info.normal[0], isect.info.normal[1], isect.info.normal[2] },
+                            0.0f };
+      hits[i] = o;
     }
   };
   lbvh::naive_thread_scheduler sched(threads);

@@ -100,6 +100,21 @@ def dump(name: str, tris: np.ndarray, rays: np.ndarray | None, R, boxes: np.ndar
     print(f"{name}: n={tris.shape[0]} rays={0 if rays is None else rays.shape[0]}")
 
 
+def dump_spheres(name: str, spheres: np.ndarray, rays: np.ndarray, R):
+    """User primitives: the example program's spheres, its sphere_to_box
+    converter (centre +- radius, float32), the reference builder over those
+    boxes, and its traverser with the example's intersector."""
+    from lbvh_gb300.api import sphere_boxes
+
+    boxes = sphere_boxes(spheres)
+    nodes = R.build_boxes(boxes, 4)
+    hits = R.trace_spheres(nodes, spheres, rays, 4)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), spheres=spheres, sphere_boxes=boxes,
+                        nodes=nodes.view(np.uint8).reshape(-1, 32), rays=rays,
+                        sphere_hits=hits.view(np.uint8).reshape(-1, 32))
+    print(f"{name}: n={spheres.shape[0]} rays={rays.shape[0]} hit={np.mean(hits['prim'] != oracle.MISS):.3f}")
+
+
 def main():
     oracle.build_libs(REF_DIR)
     R = oracle.ref()
@@ -164,6 +179,15 @@ def main():
     rad = (0.05 + 0.3 * sp[:, 3:]).astype(np.float32)
     boxes = np.concatenate([cen - rad, cen + rad], 1).astype(np.float32)
     dump("soup2000_boxes", scenes.soup(2000, 13), None, R, boxes=boxes)
+
+    # user primitives with the example program's intersector: its own three
+    # spheres under its camera, and a 2,000-sphere scene with rays from
+    # inside and outside the spheres (negative roots included)
+    dump_spheres("spheres_example", scenes.example_spheres(), scenes.example_camera_rays(96, 54), R)
+    sph = scenes.sphere_scene(2000, 21)
+    lo, hi = sph[:, 1:].min(0), sph[:, 1:].max(0)
+    rays = np.concatenate([scenes.random_rays_in_box(lo, hi, 3000, 22), scenes.pinhole_rays(40, 40, eye=(0, 0, 9))])
+    dump_spheres("spheres2000", sph, rays, R)
 
 
 if __name__ == "__main__":

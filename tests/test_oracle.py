@@ -6,7 +6,8 @@ import pytest
 
 import oracle
 from lbvh_gb300 import scenes
-from conftest import GOLDEN, hit_mismatches, load_golden, nodes_equal
+from conftest import (GOLDEN, SPHERE_GOLDEN, hit_mismatches, load_golden, load_sphere_golden, nodes_equal,
+                      sphere_hit_mismatches)
 
 
 @pytest.mark.parametrize("name", GOLDEN)
@@ -95,3 +96,19 @@ def test_port_matches_reference_boxes():
     b = scenes.uniform(3, 0, 6 * 3000).reshape(3000, 6).astype(np.float32)
     boxes = np.concatenate([np.minimum(b[:, :3], b[:, 3:]), np.maximum(b[:, :3], b[:, 3:])], 1)
     assert nodes_equal(oracle.port().build_boxes(boxes, 4), REF.build_boxes(boxes, 4))
+
+
+@pytest.mark.parametrize("name", SPHERE_GOLDEN)
+def test_port_matches_golden_spheres(port, name):
+    """User primitives: the example program's spheres, boxes from its
+    converter, the reference's builder and its traverser with the example's
+    intersector; the port agrees bit for bit (uv included: same host libm)."""
+    from lbvh_gb300.api import sphere_boxes
+
+    g = load_sphere_golden(name)
+    boxes = sphere_boxes(g["spheres"])
+    assert np.array_equal(boxes.view(np.uint32), g["sphere_boxes"].view(np.uint32))
+    assert nodes_equal(port.build_boxes(boxes, 3), g["nodes"])
+    for threads in (1, 5):
+        hits = port.trace_spheres(g["nodes"], g["spheres"], g["rays"], threads)
+        assert sphere_hit_mismatches(hits, g["sphere_hits"]).size == 0
