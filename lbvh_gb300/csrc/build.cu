@@ -276,12 +276,26 @@ k_onesweep(const uint32_t* __restrict__ kin,
       val[kPairs ? k : 0] = idx < n ? (kIotaVals ? idx : vin[idx]) : 0u;
   }
 
-  // warp-level stable ranking: items in (k, lane) order are in index order
+  // warp-level stable ranking: items in (k, lane) order are in index order.
+  // Lanes with the same digit are found with one ballot per digit bit (a
+  // cost that does not grow with the number of distinct digits in the warp;
+  // the top pass has 6-bit digits); a partial tile also masks out its
+  // non-keys.
   const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t digit_bits = pass == 3 ? 6u : 8u; // codes are 30 bits
+  const bool full_tile = base + uint32_t(kSortTile) <= n;
 #pragma unroll
   for (int k = 0; k < kSortItems; k++) {
     const uint32_t d = digit(key[k], k);
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t peers = full_tile ? 0xffffffffu : __ballot_sync(0xffffffffu, d < 256);
+#pragma unroll
+    for (uint32_t b = 0; b < 8; b++) {
+      if (b < digit_bits) {
+        const uint32_t bit = (d >> b) & 1u;
+        const uint32_t m = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? m : ~m;
+      }
+    }
     const uint32_t pre = __popc(peers & lt_mask);
     uint32_t before = 0;
     if (d < 256)
