@@ -45,6 +45,17 @@ N_BUILD_16M = 16_000_000
 BYTES_PER_PRIM = {"bounds": 36, "morton": 44, "sort": 68, "split": 20, "fit": 96}  # 264 in all
 
 
+def measured_traffic(key: str, field: str):
+    """DRAM bytes (read + write) of one launch / build from the committed
+    ncu capture summarised in profiles/ (traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return int(json.load(f)[key][field])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -212,7 +223,9 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "bytes_per_prim": sum(BYTES_PER_PRIM.values()),
-                         "traffic": None, "peak_kind": peak_kind}}
+                         "traffic": measured_traffic("build_16m", "dram_bytes_per_build") if n == N_BUILD_16M else None,
+                         "traffic_scope": "DRAM bytes of one whole build (all kernels), ncu",
+                         "peak_kind": peak_kind}}
 
 
 def _pct(xs, q):
@@ -568,7 +581,8 @@ def main():
                 "achieved": round(trace_bytes / (trace_mean * 1e-3) / 1e9, 2),
                 "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(trace_bytes / (trace_mean * 1e-3) / 1e9 / hbm_peak, 5),
-                "traffic": None, "peak_kind": peak_kind,
+                "traffic": measured_traffic("k_trace_tris", "dram_bytes_per_launch"),
+                "algorithmic_bytes": trace_bytes, "peak_kind": peak_kind,
                 "note": "traversal is latency/issue bound; see build_16m for the HBM-bound build"}
 
     # ---- served requests vs the plain path (before the large workloads) ---
