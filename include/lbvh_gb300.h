@@ -170,6 +170,12 @@ LBVH_API int lbvh_bvh_info(const lbvh_bvh* bvh, size_t* n_prims, size_t* n_nodes
 /* Replaces bvh<float>::begin()/operator[] (lbvh.h:270-292): copies the
  * (n_prims - 1) x 32-byte node array to dst (host or device). */
 LBVH_API int lbvh_bvh_nodes(lbvh_ctx* ctx, const lbvh_bvh* bvh, void* dst);
+/* Copies the primitives the BVH reads, in input order (n triangles of 48
+ * bytes, or n boxes of 24 bytes). With lbvh_bvh_nodes this is the raw dump of
+ * a BVH; lbvh_bvh_import_triangles loads such a dump back (a build in
+ * reference leaf order). No reference counterpart: the reference's bvh<float>
+ * holds only nodes and its caller keeps the primitives (lbvh.h:259-299). */
+LBVH_API int lbvh_bvh_primitives(lbvh_ctx* ctx, const lbvh_bvh* bvh, void* dst);
 /* Device address of the node array (valid until the next build/destroy). */
 LBVH_API const void* lbvh_bvh_device_nodes(const lbvh_bvh* bvh);
 /* Intermediate build arrays of a LBVH_BUILD_KEEP_CURVE build: Morton codes
@@ -287,6 +293,11 @@ LBVH_API int lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d
  * coalesced into one batched build, small traces (at most
  * trace_batch_max_rays rays) of one tree into one launch and of one batch
  * into one batched trace. A scene's requests start in submission order.
+ * An evicted scene is dumped to host memory (its nodes and triangles, as
+ * lbvh_bvh_nodes / lbvh_bvh_primitives give them) while host_budget allows,
+ * and the next trace or refit of it loads it back (lbvh_bvh_import_triangles,
+ * tree checked on the device) instead of failing with LBVH_ERR_NOT_RESIDENT;
+ * the least recently used dumps are dropped to stay within host_budget.
  * Every result equals the same request run alone through lbvh_build_triangles
  * / lbvh_refit_triangles / lbvh_trace_triangles. */
 typedef struct lbvh_server lbvh_server;
@@ -303,6 +314,7 @@ typedef struct lbvh_server_config
   size_t batch_max_tris;       /* largest build that is coalesced (0: never) */
   size_t batch_max_requests;   /* most requests in one coalesced launch */
   size_t trace_batch_max_rays; /* largest trace that is coalesced */
+  size_t host_budget;          /* bytes of host memory for evicted scenes (0: evicted scenes are dropped) */
 } lbvh_server_config;
 
 typedef struct lbvh_request_done
@@ -321,6 +333,8 @@ typedef struct lbvh_server_stats
 {
   uint64_t submitted, completed, coalesced_requests, evictions;
   uint64_t resident_scenes, resident_bytes;
+  uint64_t spills, reloads;        /* evictions kept on the host; scenes loaded back */
+  uint64_t spilled_scenes, spilled_bytes;
 } lbvh_server_stats;
 
 LBVH_API int lbvh_server_create(const lbvh_server_config* config, lbvh_server** out);

@@ -59,6 +59,7 @@ SIGNATURES = {
     "lbvh_bvh_import_triangles": (_I, [_P, _P, _S, _P, _P]),
     "lbvh_bvh_info": (_I, [_P, ctypes.POINTER(_S), ctypes.POINTER(_S), ctypes.POINTER(_U32)]),
     "lbvh_bvh_nodes": (_I, [_P, _P, _P]),
+    "lbvh_bvh_primitives": (_I, [_P, _P, _P]),
     "lbvh_bvh_device_nodes": (_P, [_P]),
     "lbvh_bvh_curve": (_I, [_P, _P, _P, _P, _P, _P]),
     "lbvh_trace_triangles": (_I, [_P, _P, _P, _S, _P]),
@@ -88,7 +89,7 @@ SIGNATURES = {
 class ServerConfig(ctypes.Structure):
     """lbvh_server_config"""
     _fields_ = [("device", _I), ("slots", _I), ("hbm_budget", _S), ("batch_max_tris", _S),
-                ("batch_max_requests", _S), ("trace_batch_max_rays", _S)]
+                ("batch_max_requests", _S), ("trace_batch_max_rays", _S), ("host_budget", _S)]
 
 
 class RequestDone(ctypes.Structure):
@@ -102,7 +103,9 @@ class ServerStats(ctypes.Structure):
     """lbvh_server_stats"""
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
                 ("coalesced_requests", ctypes.c_uint64), ("evictions", ctypes.c_uint64),
-                ("resident_scenes", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64)]
+                ("resident_scenes", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64),
+                ("spills", ctypes.c_uint64), ("reloads", ctypes.c_uint64),
+                ("spilled_scenes", ctypes.c_uint64), ("spilled_bytes", ctypes.c_uint64)]
 
 
 class LbvhError(RuntimeError):

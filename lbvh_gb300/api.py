@@ -247,6 +247,40 @@ class BVH:
         bvh._keep = triangles if _is_cuda(triangles) else None
         return bvh
 
+    def primitives(self, out=None):
+        """The primitives the BVH reads, in input order: [n, 12] float32
+        triangles or [n, 6] boxes (numpy, or written into `out`)."""
+        n, _, _ = self.info()
+        if out is None:
+            out = np.empty((n, 12 if self.kind == TRIANGLES else 6), np.float32)
+        self.ctx.check(_lib.lib().lbvh_bvh_primitives(self.ctx.handle, self._h, _addr(out)))
+        return out
+
+    # -- raw dump / reload ----------------------------------------------------
+    _MAGIC = "lbvh_gb300.bvh"
+    _VERSION = 1
+
+    def save(self, path) -> None:
+        """Writes the raw dump of a triangle BVH built in reference leaf
+        order: the node array (the reference's 32-byte nodes) and the
+        triangles, as an .npz file. BVH.load reads it back."""
+        n, _, flags = self.info()
+        if self.kind != TRIANGLES or flags & _lib.LBVH_BUILD_SORTED_LEAVES:
+            raise ValueError("save() writes triangle BVHs in reference leaf order")
+        np.savez(path, magic=np.array(self._MAGIC), version=np.array(self._VERSION, np.int32),
+                 nodes=self.nodes().view(np.uint8).reshape(-1, 32), triangles=self.primitives())
+
+    @classmethod
+    def load(cls, path, ctx: Context | None = None) -> "BVH":
+        """Reads a dump written by save(); the node array is checked on the
+        device before the BVH can be traced (from_nodes)."""
+        with np.load(path) as f:
+            if str(f["magic"]) != cls._MAGIC or int(f["version"]) != cls._VERSION:
+                raise ValueError(f"{path} is not a BVH dump of this library (version {cls._VERSION})")
+            nodes = np.ascontiguousarray(f["nodes"]).reshape(-1).view(NODE_DTYPE)
+            tris = np.ascontiguousarray(f["triangles"], dtype=np.float32)
+        return cls.from_nodes(nodes, tris, ctx)
+
     def refit(self, primitives):
         """Recompute all node boxes over moved primitives (same count and
         order as the build input), keeping the topology."""

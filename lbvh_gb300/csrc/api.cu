@@ -711,6 +711,22 @@ lbvh_bvh_nodes(lbvh_ctx* c, const lbvh_bvh* b, void* dst)
   return host ? check_device(c) : LBVH_OK;
 }
 
+int
+lbvh_bvh_primitives(lbvh_ctx* c, const lbvh_bvh* b, void* dst)
+{
+  if (!c || !b || !dst)
+    return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (b->n < 2 || !b->prims)
+    return fail(c, LBVH_ERR_INVALID_ARG, "BVH has not been built");
+  int st = set_device(c);
+  if (st)
+    return st;
+  const size_t rec = b->kind == kKindTris ? sizeof(Tri) : sizeof(Box);
+  const bool host = !on_device(dst);
+  CK(cudaMemcpyAsync(dst, b->prims, rec * b->n, cudaMemcpyDefault, c->stream), "primitive copy");
+  return host ? check_device(c) : LBVH_OK;
+}
+
 const void*
 lbvh_bvh_device_nodes(const lbvh_bvh* b)
 {

@@ -9,6 +9,8 @@
 //   * a worker runs one job at a time on its own stream and context (copies,
 //     launches through the public C ABI, then a context synchronize), touches
 //     only the job and its own staging buffers, and hands the job back;
+//   * a spill thread (own stream and context) copies evicted scenes to host
+//     memory, in eviction order, and hands the dumps back the same way;
 //   * wait_any() (any thread) takes finished requests from the done list.
 // Device memory of resident scenes is allocated by the worker that builds
 // it (stream-ordered) and freed by the dispatch thread on its own release
@@ -76,6 +78,17 @@ struct Resident
 };
 using ResPtr = std::shared_ptr<Resident>;
 
+// An evicted scene kept on the host: the raw dump of its tree.
+struct Spilled
+{
+  size_t n = 0;                       // triangles
+  std::vector<unsigned char> nodes;   // (n - 1) x 32-byte reference nodes
+  std::vector<float> tris;            // n x 12 floats
+  uint64_t last_use = 0;
+  size_t bytes() const { return nodes.size() + 4 * tris.size(); }
+};
+using SpillPtr = std::shared_ptr<Spilled>;
+
 struct Worker;
 
 enum class JobKind
@@ -83,7 +96,9 @@ enum class JobKind
   build,
   batch_build,
   refit,
-  trace
+  trace,
+  spill,  // copy an evicted scene to the host (the spill thread)
+  reload  // load a spilled scene back onto the device
 };
 
 struct Job
@@ -98,6 +113,8 @@ struct Job
   std::vector<ResPtr> used;                     // trace: every scene read, one per request
   size_t rays = 0;                              // trace: rays in the launch
   Worker* worker = nullptr;                     // the worker that runs it
+  int64_t scene = 0;                            // spill / reload: the scene
+  SpillPtr dump;                                // spill: filled; reload: read
   // results of the worker
   lbvh_bvh* bvh = nullptr;
   lbvh_batch* batch = nullptr;
@@ -139,17 +156,24 @@ struct lbvh_server
   std::vector<int64_t> resident_snapshot;
   uint64_t next_ticket = 1, next_seq = 0, submitted = 0, completed = 0;
   uint64_t coalesced = 0, evictions = 0, used_snapshot = 0;
+  uint64_t spills = 0, reloads = 0, spilled_snapshot = 0, host_used_snapshot = 0;
+  std::deque<JobPtr> spill_jobs; // for the spill thread
   bool dirty = false, stop = false;
   // dispatch thread only
   std::unordered_map<int64_t, std::deque<ReqPtr>> queues;
   std::unordered_map<int64_t, ResPtr> resident;
   std::unordered_set<int64_t> writing;
   std::vector<lbvh_request_done> outbox; // reports of this step
+  std::unordered_map<int64_t, SpillPtr> spilled; // evicted scenes kept on the host
+  std::unordered_set<int64_t> spilling;          // evictions being copied out
+  size_t host_used = 0;
+  uint64_t spill_inflight = 0;
   size_t used = 0;
   uint64_t tick = 0;
   cudaStream_t release_stream = nullptr;
   lbvh_ctx* release_ctx = nullptr;
   std::vector<std::unique_ptr<Worker>> workers;
+  std::unique_ptr<Worker> spiller; // copies evicted scenes out, off the workers' streams
   std::thread dispatcher;
 
   double now() const
@@ -319,6 +343,39 @@ run_trace(Worker& w, Job& j)
   return true;
 }
 
+bool
+run_spill(Worker& w, Job& j)
+{
+  const Resident& r = *j.res;
+  auto d = std::make_shared<Spilled>();
+  d->n = r.n;
+  d->nodes.resize(kNodeBytes * (r.n - 1));
+  d->tris.resize(12 * r.n);
+  if (r.batch) {
+    const BatchRef& b = *r.batch;
+    W_LB(lbvh_batch_mesh_nodes(w.ctx, b.batch, r.index, d->nodes.data()), "member node dump");
+    W_CK(cudaMemcpyAsync(d->tris.data(), static_cast<const char*>(b.tris) + kTriBytes * b.off[r.index],
+                         kTriBytes * r.n, cudaMemcpyDeviceToHost, w.stream),
+         "member triangle dump");
+  } else {
+    W_LB(lbvh_bvh_nodes(w.ctx, r.bvh, d->nodes.data()), "node dump");
+    W_LB(lbvh_bvh_primitives(w.ctx, r.bvh, d->tris.data()), "triangle dump");
+  }
+  j.dump = std::move(d);
+  return true;
+}
+
+bool
+run_reload(Worker& w, Job& j)
+{
+  const Spilled& d = *j.dump;
+  W_LB(lbvh_bvh_create(w.ctx, &j.bvh), "bvh create");
+  // host triangles are copied into memory the BVH owns; the tree is checked
+  W_LB(lbvh_bvh_import_triangles(w.ctx, d.nodes.data(), d.n - 1, d.tris.data(), j.bvh), "reload");
+  W_LB(lbvh_bvh_prepare_trace(w.ctx, j.bvh), "prepare trace");
+  return true;
+}
+
 #undef W_CK
 #undef W_LB
 
@@ -350,6 +407,12 @@ worker_loop(lbvh_server* s, Worker* w)
       case JobKind::trace:
         ok = run_trace(*w, j);
         break;
+      case JobKind::spill:
+        ok = run_spill(*w, j);
+        break;
+      case JobKind::reload:
+        ok = run_reload(*w, j);
+        break;
     }
     // waits for the stream and reads the context's device error word
     const int st = lbvh_ctx_synchronize(w->ctx);
@@ -358,6 +421,34 @@ worker_loop(lbvh_server* s, Worker* w)
     j.t_done = s->now();
     std::lock_guard<std::mutex> lk(s->mu);
     w->job.reset();
+    s->finished.push_back(job);
+    s->dirty = true;
+    s->cv_dispatch.notify_one();
+  }
+}
+
+// The spill thread: takes spill jobs in order from the server's queue, on its
+// own stream and context, and hands them back like a worker.
+void
+spill_loop(lbvh_server* s, Worker* w)
+{
+  cudaSetDevice(s->cfg.device);
+  for (;;) {
+    JobPtr job;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      w->cv.wait(lk, [&] { return !s->spill_jobs.empty() || w->quit; });
+      if (s->spill_jobs.empty())
+        return;
+      job = s->spill_jobs.front();
+      s->spill_jobs.pop_front();
+    }
+    bool ok = run_spill(*w, *job);
+    const int st = lbvh_ctx_synchronize(w->ctx);
+    if (ok && st != LBVH_OK)
+      fail_job(*job, w->ctx, st, "device");
+    job->t_done = s->now();
+    std::lock_guard<std::mutex> lk(s->mu);
     s->finished.push_back(job);
     s->dirty = true;
     s->cv_dispatch.notify_one();
@@ -410,6 +501,50 @@ drop(lbvh_server* s, int64_t scene)
     release(s, *r);
 }
 
+// Moves a resident scene out of the device budget towards the host: the
+// spill thread copies its tree out, then its device memory is freed (no
+// running job reads it: eviction picks idle scenes only).
+void
+start_spill(lbvh_server* s, int64_t scene)
+{
+  auto it = s->resident.find(scene);
+  ResPtr r = it->second;
+  s->resident.erase(it);
+  s->used -= r->nbytes; // out of the budget now; its memory goes when the copy is done
+  r->nbytes = 0;
+  r->retired = true;
+  s->spilling.insert(scene);
+  s->spill_inflight++;
+  auto job = std::make_shared<Job>();
+  job->kind = JobKind::spill;
+  job->res = r;
+  job->scene = scene;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->spill_jobs.push_back(std::move(job));
+  s->spiller->cv.notify_one();
+}
+
+void
+evict(lbvh_server* s, int64_t scene)
+{
+  const ResPtr& r = s->resident.at(scene);
+  const size_t dump = kNodeBytes * (r->n - 1) + kTriBytes * r->n;
+  if (s->cfg.host_budget && dump <= s->cfg.host_budget)
+    start_spill(s, scene);
+  else
+    drop(s, scene);
+}
+
+void
+forget_spilled(lbvh_server* s, int64_t scene)
+{
+  auto it = s->spilled.find(scene);
+  if (it == s->spilled.end())
+    return;
+  s->host_used -= it->second->bytes();
+  s->spilled.erase(it);
+}
+
 bool
 make_room(lbvh_server* s, size_t need, int64_t keep)
 {
@@ -424,7 +559,7 @@ make_room(lbvh_server* s, size_t need, int64_t keep)
   for (auto& e : lru) {
     if (s->used + need <= s->cfg.hbm_budget)
       break;
-    drop(s, e.second);
+    evict(s, e.second);
     evicted++;
   }
   if (evicted) {
@@ -437,7 +572,7 @@ make_room(lbvh_server* s, size_t need, int64_t keep)
 bool
 admissible(lbvh_server* s, const Request& r)
 {
-  if (s->writing.count(r.scene))
+  if (s->writing.count(r.scene) || s->spilling.count(r.scene))
     return false;
   auto it = s->resident.find(r.scene);
   if (r.kind == LBVH_REQ_TRACE)
@@ -529,6 +664,19 @@ start_refit(lbvh_server* s, Worker* w, const ReqPtr& r)
   launch(s, w, std::move(job));
 }
 
+// Loads a spilled scene back; its requests wait (the scene is "writing").
+void
+start_reload(lbvh_server* s, Worker* w, int64_t scene)
+{
+  auto job = std::make_shared<Job>();
+  job->kind = JobKind::reload;
+  job->scene = scene;
+  job->dump = s->spilled.at(scene);
+  s->used += scene_bytes(job->dump->n);
+  s->writing.insert(scene);
+  launch(s, w, std::move(job));
+}
+
 void
 start_trace(lbvh_server* s, Worker* w, std::vector<ReqPtr> group)
 {
@@ -592,11 +740,21 @@ dispatch(lbvh_server* s)
   ReqPtr chosen;
   for (auto& h : heads) {
     const ReqPtr& r = s->queues[h.second].front();
+    if (s->spilling.count(r->scene))
+      continue; // its tree is being copied out; then it can be loaded back
     auto it = s->resident.find(r->scene);
     const bool known = it != s->resident.end() || s->writing.count(r->scene);
     if (r->kind != LBVH_REQ_BUILD && !known) {
-      reject(s, r, LBVH_ERR_NOT_RESIDENT, "scene " + std::to_string(r->scene) + " is not resident");
-      return true;
+      auto sp = s->spilled.find(r->scene);
+      if (sp == s->spilled.end()) {
+        reject(s, r, LBVH_ERR_NOT_RESIDENT, "scene " + std::to_string(r->scene) + " is not resident");
+        return true;
+      }
+      if (make_room(s, scene_bytes(sp->second->n), r->scene)) {
+        start_reload(s, w, r->scene);
+        return true;
+      }
+      continue;
     }
     if (r->kind == LBVH_REQ_REFIT && it != s->resident.end() && !s->writing.count(r->scene) &&
         it->second->n != r->rows) {
@@ -701,6 +859,7 @@ finish(lbvh_server* s, Job& j)
           continue;
         }
         drop(s, r->scene); // the tree this build replaces
+        forget_spilled(s, r->scene);
         auto res = std::make_shared<Resident>();
         res->n = r->rows;
         res->nbytes = j.nbytes[k];
@@ -739,6 +898,50 @@ finish(lbvh_server* s, Job& j)
       res->last_use = ++s->tick;
       break;
     }
+    case JobKind::spill: {
+      s->spill_inflight--;
+      s->spilling.erase(j.scene);
+      release(s, *j.res); // the device copy goes (nothing of it was still counted)
+      if (!ok || !j.dump)
+        break; // the scene is gone, as a dropped one is
+      const size_t b = j.dump->bytes();
+      while (s->host_used + b > s->cfg.host_budget) { // drop the least recently used dumps
+        auto lru = s->spilled.end();
+        for (auto it = s->spilled.begin(); it != s->spilled.end(); ++it)
+          if (!s->writing.count(it->first) && (lru == s->spilled.end() || it->second->last_use < lru->second->last_use))
+            lru = it; // (a dump being loaded back stays)
+        if (lru == s->spilled.end())
+          break;
+        forget_spilled(s, lru->first);
+      }
+      if (s->host_used + b <= s->cfg.host_budget) {
+        j.dump->last_use = ++s->tick;
+        s->spilled[j.scene] = j.dump;
+        s->host_used += b;
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->spills++;
+      }
+      break;
+    }
+    case JobKind::reload: {
+      s->writing.erase(j.scene);
+      const size_t nb = scene_bytes(j.dump->n);
+      forget_spilled(s, j.scene);
+      if (!ok) { // the dump did not load: the scene is gone
+        s->used -= nb;
+        free_job_outputs(s, j);
+        break;
+      }
+      auto res = std::make_shared<Resident>();
+      res->n = j.dump->n;
+      res->nbytes = nb;
+      res->bvh = j.bvh; // owns its triangles
+      res->last_use = ++s->tick;
+      s->resident[j.scene] = res;
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->reloads++;
+      break;
+    }
     case JobKind::trace:
       for (const ResPtr& res : j.used) {
         res->busy--;
@@ -755,6 +958,8 @@ finish(lbvh_server* s, Job& j)
 bool
 any_busy(const lbvh_server* s)
 {
+  if (s->spill_inflight)
+    return true;
   for (const auto& w : s->workers)
     if (w->busy)
       return true;
@@ -791,6 +996,10 @@ dispatcher_loop(lbvh_server* s)
             w->quit = true;
             w->cv.notify_one();
           }
+          if (s->spiller) {
+            s->spiller->quit = true;
+            s->spiller->cv.notify_one();
+          }
           return;
         }
         s->cv_dispatch.wait(lk);
@@ -802,7 +1011,8 @@ dispatcher_loop(lbvh_server* s)
     for (ReqPtr& r : inbox)
       s->queues[r->scene].push_back(std::move(r));
     for (JobPtr& j : fin) {
-      j->worker->busy = false;
+      if (j->worker) // spill jobs run on the spill thread
+        j->worker->busy = false;
       finish(s, *j);
     }
     while (dispatch(s)) {
@@ -818,6 +1028,8 @@ dispatcher_loop(lbvh_server* s)
     std::lock_guard<std::mutex> lk(s->mu);
     s->resident_snapshot.swap(snap);
     s->used_snapshot = s->used;
+    s->spilled_snapshot = s->spilled.size();
+    s->host_used_snapshot = s->host_used;
     if (!s->outbox.empty()) {
       s->done.insert(s->done.end(), s->outbox.begin(), s->outbox.end());
       s->completed += s->outbox.size();
@@ -834,9 +1046,20 @@ destroy_all(lbvh_server* s)
     if (w->thread.joinable())
       w->thread.join();
   }
+  if (s->spiller && s->spiller->thread.joinable())
+    s->spiller->thread.join();
   for (auto& kv : s->resident)
     release(s, *kv.second);
   s->resident.clear();
+  s->spilled.clear();
+  if (s->spiller) {
+    if (s->spiller->ctx)
+      lbvh_ctx_destroy(s->spiller->ctx);
+    if (s->spiller->stream) {
+      cudaStreamSynchronize(s->spiller->stream);
+      cudaStreamDestroy(s->spiller->stream);
+    }
+  }
   for (auto& w : s->workers) {
     if (w->rays)
       cudaFreeAsync(w->rays, w->stream);
@@ -897,8 +1120,20 @@ lbvh_server_create(const lbvh_server_config* cfg, lbvh_server** out)
       }
       s->workers.push_back(std::move(w));
     }
+    {
+      auto w = std::make_unique<Worker>();
+      w->index = -1;
+      const bool ok = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) == cudaSuccess &&
+                      lbvh_ctx_create(cfg->device, w->stream, &w->ctx) == LBVH_OK;
+      s->spiller = std::move(w);
+      if (!ok) {
+        destroy_all(s);
+        return LBVH_ERR_DEVICE;
+      }
+    }
     for (auto& w : s->workers)
       w->thread = std::thread(worker_loop, s, w.get());
+    s->spiller->thread = std::thread(spill_loop, s, s->spiller.get());
     s->dispatcher = std::thread(dispatcher_loop, s);
   } catch (...) { // thread or allocation failure
     if (s) {
@@ -909,6 +1144,10 @@ lbvh_server_create(const lbvh_server_config* cfg, lbvh_server** out)
         for (auto& w : s->workers) {
           w->quit = true;
           w->cv.notify_one();
+        }
+        if (s->spiller) {
+          s->spiller->quit = true;
+          s->spiller->cv.notify_one();
         }
         s->cv_dispatch.notify_one();
       }
@@ -994,6 +1233,10 @@ lbvh_server_stats_get(lbvh_server* s, lbvh_server_stats* out)
   out->evictions = s->evictions;
   out->resident_scenes = s->resident_snapshot.size();
   out->resident_bytes = s->used_snapshot;
+  out->spills = s->spills;
+  out->reloads = s->reloads;
+  out->spilled_scenes = s->spilled_snapshot;
+  out->spilled_bytes = s->host_used_snapshot;
   return LBVH_OK;
 }
 

@@ -11,7 +11,9 @@ request at a time):
 * every scene's BVH stays resident on the device between requests;
 * admission is against an HBM budget: a request that needs memory evicts
   least-recently-used resident scenes that no queued or running request
-  needs, and otherwise waits until running work frees memory;
+  needs, and otherwise waits until running work frees memory; an evicted
+  scene's tree is dumped to host memory (within `host_budget`) and loaded
+  back, checked, by its next trace or refit;
 * small builds (at most `batch_max_tris` triangles) waiting together are
   coalesced into one batched build (lbvh_batch_build_triangles); small
   traces queued together against one tree become one trace launch, and those
@@ -88,10 +90,10 @@ class Server:
 
     def __init__(self, device: int = 0, slots: int = 4, hbm_budget: int = 120 << 30,
                  batch_max_tris: int = 65536, batch_max_requests: int = 128,
-                 trace_batch_max_rays: int = 1 << 16):
+                 trace_batch_max_rays: int = 1 << 16, host_budget: int = 64 << 30):
         L = _lib.lib()
         cfg = _lib.ServerConfig(int(device), int(slots), int(hbm_budget), int(batch_max_tris),
-                                int(batch_max_requests), int(trace_batch_max_rays))
+                                int(batch_max_requests), int(trace_batch_max_rays), int(host_budget))
         h = ctypes.c_void_p()
         st = L.lbvh_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if st:
@@ -165,6 +167,20 @@ class Server:
     @property
     def evictions(self) -> int:
         return int(self._stats().evictions)
+
+    @property
+    def spills(self) -> int:
+        """Evicted scenes dumped to host memory."""
+        return int(self._stats().spills)
+
+    @property
+    def reloads(self) -> int:
+        """Dumped scenes loaded back onto the device."""
+        return int(self._stats().reloads)
+
+    @property
+    def spilled(self) -> int:
+        return int(self._stats().spilled_scenes)
 
     @property
     def used(self) -> int:

@@ -130,3 +130,29 @@ def test_full_size_16m_build_parity(ctx, port):
     nodes = lb.Builder(ctx)(d).nodes()
     assert nodes_equal(nodes, port.build(t, 16))
     assert port.check_bvh(nodes) == 0
+
+
+def test_dump_and_reload_round_trip(lib_built, tmp_path):
+    """A BVH written with save() and read back with load() has the same
+    nodes and primitives and traces to the same hits; a dump of a sorted-leaf
+    tree is refused, and a corrupted node array is rejected on reload."""
+    t = scenes.torus_scene(seed=12)
+    bvh = lb.Builder()(t)
+    p = tmp_path / "scene.npz"
+    bvh.save(p)
+    back = lb.BVH.load(p)
+    assert np.array_equal(back.nodes().view(np.uint8), bvh.nodes().view(np.uint8))
+    assert np.array_equal(back.primitives().view(np.uint32), t.view(np.uint32))
+    rays = scenes.incoherent_rays(t, 4096, 13)
+    a = lb.Traverser(bvh)(rays)
+    b = lb.Traverser(back)(rays)
+    assert a.tobytes() == b.tobytes()
+    with pytest.raises(ValueError):
+        lb.Builder(sorted_leaves=True)(t).save(tmp_path / "sorted.npz")
+    d = dict(np.load(p))
+    nodes = d["nodes"].reshape(-1).view(lb.NODE_DTYPE).copy()
+    nodes["left"][5] = nodes["left"][6]  # two parents for one child
+    d["nodes"] = nodes.view(np.uint8).reshape(-1, 32)
+    np.savez(tmp_path / "bad.npz", **d)
+    with pytest.raises(lb.LbvhError):
+        lb.BVH.load(tmp_path / "bad.npz")

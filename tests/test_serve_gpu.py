@@ -46,7 +46,7 @@ def test_eviction_under_a_small_budget(lib_built):
     # scene without queued work; the scenes still resident trace correctly
     meshes = [scenes.torus_mesh(40_000, 50 + k) for k in range(10)]
     budget = 4 * scene_bytes(meshes[0].shape[0]) + 1024
-    with Server(slots=2, hbm_budget=budget, batch_max_tris=0) as srv:
+    with Server(slots=2, hbm_budget=budget, batch_max_tris=0, host_budget=0) as srv:
         for k, m in enumerate(meshes):
             srv.submit("build", k, m).result(timeout=60)
         assert srv.evictions >= 6
@@ -85,3 +85,38 @@ def test_rejected_requests_leave_the_server_usable(lib_built):
         got = srv.submit("trace", 3, rays).result(timeout=30)
     want = run_plain([(0.0, "build", 3, t), (0.0, "trace", 3, rays)])[1][0]
     assert hit_mismatches(got, want).size == 0
+
+
+def test_evicted_scenes_are_dumped_and_reloaded(lib_built):
+    """With a host budget, an evicted scene's tree goes to host memory and
+    its next trace loads it back: the hits equal a fresh build's, and a refit
+    of a reloaded scene works as on any resident tree. When the host budget
+    is full, the least recently used dump is dropped: that scene is gone."""
+    import time
+
+    meshes = [scenes.torus_mesh(30_000, 60 + k) for k in range(8)]
+    each = scene_bytes(meshes[0].shape[0])
+    dump = 32 * (meshes[0].shape[0] - 1) + 48 * meshes[0].shape[0]
+    rays = [scenes.incoherent_rays(m, 5_000, 70 + k) for k, m in enumerate(meshes)]
+    moved = scenes.jitter(meshes[3], 5, 0.01)
+    with Server(slots=2, hbm_budget=3 * each + 1024, batch_max_tris=0, host_budget=4 * dump + 1024) as srv:
+        for k, m in enumerate(meshes):
+            srv.submit("build", k, m).result(timeout=60)
+        deadline = time.time() + 30
+        while srv.spills < 5 and time.time() < deadline:  # dumps are copied out asynchronously
+            time.sleep(0.01)
+        assert srv.evictions == 5 and srv.spills == 5 and srv.spilled == 4
+        with pytest.raises(KeyError):  # the oldest dump fell out of the host budget
+            srv.submit("trace", 0, rays[0]).result(timeout=60)
+        got1 = srv.submit("trace", 1, rays[1]).result(timeout=60)  # loaded back
+        assert srv.reloads == 1
+        got3 = srv.submit("trace", 3, rays[3]).result(timeout=60)
+        srv.submit("refit", 3, moved).result(timeout=60)
+        got3b = srv.submit("trace", 3, rays[3]).result(timeout=60)
+        assert srv.reloads == 2
+    want1 = run_plain([(0.0, "build", 1, meshes[1]), (0.0, "trace", 1, rays[1])])[1][0]
+    want3 = run_plain([(0.0, "build", 3, meshes[3]), (0.0, "trace", 3, rays[3]),
+                       (0.0, "refit", 3, moved), (0.0, "trace", 3, rays[3])])
+    assert hit_mismatches(got1, want1).size == 0
+    assert hit_mismatches(got3, want3[1][0]).size == 0
+    assert hit_mismatches(got3b, want3[3][0]).size == 0
