@@ -432,6 +432,37 @@ def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_
     res["plain_step_ms"] = round(plain_ms, 3)
     best = res["graph_step_ms"] or res["step_ms"]
     res["speedup_vs_plain"] = round(plain_ms / best, 2)
+    # the same meshes with sorted leaves (each mesh's leaves in stable Morton
+    # order): the intended LBVH, whose trees stay tight for randomly ordered
+    # input; hits are checked against the plain sorted-leaf path on a sample
+    with torch.cuda.stream(s):
+        sb = lb.Batch(ctx)
+        sout = torch.empty_like(out)
+        for _ in range(3):
+            sb.build(tris, off, sorted_leaves=True)
+            sb.trace(rays, roff, out=sout)
+        torch.cuda.synchronize()
+        sbt, stt = [], []
+        for _ in range(max(3, min(steps, 10))):
+            flush.zero_()
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            e[0].record(s)
+            sb.build(tris, off, sorted_leaves=True)
+            e[1].record(s)
+            sb.trace(rays, roff, out=sout)
+            e[2].record(s)
+            torch.cuda.synchronize()
+            sbt.append(e[0].elapsed_time(e[1]))
+            stt.append(e[1].elapsed_time(e[2]))
+        sbuilder = lb.Builder(ctx, sorted_leaves=True)
+        for k in range(0, n_meshes, max(1, n_meshes // 16)):
+            r0, r1 = int(roff_h[k]), int(roff_h[k + 1])
+            want = lb.Traverser(sbuilder(tris[int(off_h[k]):int(off_h[k + 1])]))(rays[r0:r1])
+            torch.cuda.synchronize()
+            assert torch.equal(want.view(torch.int32), sout[r0:r1].view(torch.int32))
+    sbm, stm = float(np.mean(sbt)), float(np.mean(stt))
+    res["sorted_leaves"] = {"build_ms": round(sbm, 3), "trace_ms": round(stm, 3), "step_ms": round(sbm + stm, 3),
+                            "trace_mrays_s": round(res["rays"] / (stm * 1e-3) / 1e6, 1)}
     del tris, rays, out, flush
     torch.cuda.empty_cache()
     return res

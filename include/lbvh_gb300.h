@@ -239,6 +239,12 @@ LBVH_API int lbvh_batch_destroy(lbvh_ctx* ctx, lbvh_batch* batch);
  * array is reported as LBVH_ERR_BAD_TOPOLOGY by the next synchronizing call. */
 LBVH_API int lbvh_batch_build_triangles(lbvh_ctx* ctx, const float* tris, size_t total, const uint32_t* offsets,
                                         size_t n_meshes, lbvh_batch* batch);
+/* lbvh_batch_build_triangles with build flags: 0 (reference leaf order, as
+ * above) or LBVH_BUILD_SORTED_LEAVES, in which each mesh's node block equals
+ * lbvh_build_triangles(..., LBVH_BUILD_SORTED_LEAVES) of that mesh alone and
+ * lbvh_batch_trace_triangles reports mesh-local ids in input order. */
+LBVH_API int lbvh_batch_build(lbvh_ctx* ctx, const float* tris, size_t total, const uint32_t* offsets, size_t n_meshes,
+                              uint32_t flags, lbvh_batch* batch);
 LBVH_API int lbvh_batch_info(const lbvh_batch* batch, size_t* n_meshes, size_t* total_prims, size_t* total_nodes);
 /* As lbvh_bvh_prepare_trace, for a batch. */
 LBVH_API int lbvh_batch_prepare_trace(lbvh_ctx* ctx, lbvh_batch* batch);

@@ -71,6 +71,7 @@ SIGNATURES = {
     "lbvh_batch_create": (_I, [_P, _PP]),
     "lbvh_batch_destroy": (_I, [_P, _P]),
     "lbvh_batch_build_triangles": (_I, [_P, _P, _S, _P, _S, _P]),
+    "lbvh_batch_build": (_I, [_P, _P, _S, _P, _S, _U32, _P]),
     "lbvh_batch_info": (_I, [_P, ctypes.POINTER(_S), ctypes.POINTER(_S), ctypes.POINTER(_S)]),
     "lbvh_batch_nodes": (_I, [_P, _P, _P]),
     "lbvh_batch_trace_triangles": (_I, [_P, _P, _P, _P, _S, _P]),

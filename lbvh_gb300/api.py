@@ -462,14 +462,18 @@ class Batch:
         self._offsets = None
         self._offsets_host = None
 
-    def build(self, triangles, offsets) -> "Batch":
+    def build(self, triangles, offsets, sorted_leaves: bool = False) -> "Batch":
+        """Builds every mesh [offsets[k], offsets[k + 1]) in one launch; with
+        sorted_leaves=True each mesh's tree is the sorted-leaf build of that
+        mesh (leaves in stable Morton order; hits report input-order ids)."""
         offsets = _u32(offsets, "offsets")
         n_meshes = (offsets.size if isinstance(offsets, np.ndarray) else offsets.numel()) - 1
         total = _rows(triangles, 12, "triangles")
         if n_meshes < 1:
             raise ValueError("need at least one mesh")
-        self.ctx.check(_lib.lib().lbvh_batch_build_triangles(self.ctx.handle, _addr(triangles), total,
-                                                            _addr(offsets), n_meshes, self._h))
+        flags = _lib.LBVH_BUILD_SORTED_LEAVES if sorted_leaves else 0
+        self.ctx.check(_lib.lib().lbvh_batch_build(self.ctx.handle, _addr(triangles), total, _addr(offsets),
+                                                  n_meshes, flags, self._h))
         self._keep = (triangles, offsets)
         self._offsets = offsets  # read back lazily: build() stays free of host syncs
         self._offsets_host = None

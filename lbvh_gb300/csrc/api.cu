@@ -928,6 +928,9 @@ struct lbvh_batch
   DevBuf wnodes;             // traversal copy + flag word
   bool wnodes_valid = false;
   std::vector<uint32_t> host_off; // host copy of the offsets when they were given on the host
+  uint32_t flags = 0;
+  DevBuf sorted_tris;        // sorted-leaf mode: each mesh's triangles in leaf order
+  DevBuf leaf_prim;          // sorted-leaf mode: mesh-local triangle id of each leaf slot
 };
 
 namespace {
@@ -1001,6 +1004,8 @@ lbvh_batch_destroy(lbvh_ctx* c, lbvh_batch* b)
   release(b->tris_owned, c->stream);
   release(b->nodes, c->stream);
   release(b->wnodes, c->stream);
+  release(b->sorted_tris, c->stream);
+  release(b->leaf_prim, c->stream);
   delete b;
   return LBVH_OK;
 }
@@ -1009,8 +1014,18 @@ int
 lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const uint32_t* offsets, size_t n_meshes,
                            lbvh_batch* b)
 {
+  return lbvh_batch_build(c, tris, total, offsets, n_meshes, 0, b);
+}
+
+int
+lbvh_batch_build(lbvh_ctx* c, const float* tris, size_t total, const uint32_t* offsets, size_t n_meshes,
+                 uint32_t flags, lbvh_batch* b)
+{
   if (!c || !tris || !offsets || !b)
     return fail(c, LBVH_ERR_INVALID_ARG, "null argument");
+  if (flags & ~LBVH_BUILD_SORTED_LEAVES)
+    return fail(c, LBVH_ERR_INVALID_ARG, "unsupported batch build flags 0x%x", flags);
+  const bool sorted = flags & LBVH_BUILD_SORTED_LEAVES;
   if (n_meshes < 1 || total < 2 * n_meshes || total > kMaxPrims)
     return fail(c, LBVH_ERR_INVALID_ARG, "%zu meshes over %zu triangles", n_meshes, total);
   int st = set_device(c);
@@ -1039,8 +1054,13 @@ lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const u
   const size_t o_keys_a = align_up(24 * total, 256);
   const size_t o_keys_b = o_keys_a + align_up(4 * total, 256);
   const size_t o_slots = o_keys_b + align_up(4 * total, 256);
-  const size_t ws_bytes = o_slots + align_up(4 * total, 256);
+  const size_t o_vals_b = o_slots + align_up(4 * total, 256);
+  const size_t ws_bytes = o_vals_b + (sorted ? align_up(4 * total, 256) : 0);
   CK(reserve(c->batch_ws, ws_bytes, c->stream), "batch workspace allocation");
+  if (sorted) {
+    CK(reserve(b->sorted_tris, sizeof(Tri) * total, c->stream), "sorted triangle allocation");
+    CK(reserve(b->leaf_prim, 4 * total, c->stream), "leaf map allocation");
+  }
   char* ws = static_cast<char*>(c->batch_ws.ptr);
   BatchBuffers bb{};
   bb.off = static_cast<const uint32_t*>(b->off.ptr);
@@ -1052,6 +1072,11 @@ lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const u
   bb.keys_b = reinterpret_cast<uint32_t*>(ws + o_keys_b);
   bb.slots = reinterpret_cast<uint32_t*>(ws + o_slots);
   bb.error = &c->state->error;
+  if (sorted) { // the permutation lands in the batch's own leaf map
+    bb.vals_a = static_cast<uint32_t*>(b->leaf_prim.ptr);
+    bb.vals_b = reinterpret_cast<uint32_t*>(ws + o_vals_b);
+    bb.sorted_tris = static_cast<Tri*>(b->sorted_tris.ptr);
+  }
   CK(launch_batch_build(static_cast<const Tri*>(dt), bb, static_cast<Node*>(b->nodes.ptr), c->batch_threads,
                         c->num_sms, c->stream),
      "batch build launch");
@@ -1060,6 +1085,7 @@ lbvh_batch_build_triangles(lbvh_ctx* c, const float* tris, size_t total, const u
   b->tris = dt;
   b->device = c->device;
   b->wnodes_valid = false;
+  b->flags = flags;
   return host ? check_device(c) : LBVH_OK;
 }
 
@@ -1172,7 +1198,10 @@ lbvh_batch_trace_triangles(lbvh_ctx* c, const lbvh_batch* b, const float* rays, 
   } else if (reinterpret_cast<uintptr_t>(hits) & 15) {
     return fail(c, LBVH_ERR_INVALID_ARG, "device hits must be 16-byte aligned");
   }
-  CK(launch_batch_trace(static_cast<const WideNode*>(mb->wnodes.ptr), total_nodes, static_cast<const Tri*>(b->tris),
+  const bool sorted = b->flags & LBVH_BUILD_SORTED_LEAVES;
+  CK(launch_batch_trace(static_cast<const WideNode*>(mb->wnodes.ptr), total_nodes,
+                        static_cast<const Tri*>(sorted ? b->sorted_tris.ptr : b->tris),
+                        sorted ? static_cast<const uint32_t*>(b->leaf_prim.ptr) : nullptr,
                         static_cast<const uint32_t*>(b->off.ptr), droff,
                         b->n_meshes, dr, uint32_t(m), dh, c->ray_counter, c->num_sms, c->trace, c->stream),
      "batch trace launch");

@@ -20,6 +20,7 @@
 #include "device_util.cuh"
 
 #include <atomic>
+#include <type_traits>
 
 namespace lbvh_gb300 {
 
@@ -38,6 +39,14 @@ struct CgBoxLeaf
     const float2 a = __ldcg(p), b = __ldcg(p + 1), c = __ldcg(p + 2);
     return Box{ { a.x, a.y, b.x }, { b.y, c.x, c.y } };
   }
+};
+
+// Sorted-leaf mode: the box of leaf slot j is that of triangle perm[j].
+struct CgPermBoxLeaf
+{
+  const Box* boxes;
+  const uint32_t* perm;
+  __device__ __forceinline__ Box operator()(uint32_t j) const { return CgBoxLeaf{ boxes }(__ldcg(perm + j)); }
 };
 
 __device__ __forceinline__ int
@@ -87,6 +96,7 @@ scan256(uint32_t v, uint32_t* s_tmp)
 
 // One CTA per mesh at a time (see the file comment). Dynamic shared memory:
 // one 256-counter histogram per warp for the chunk ranking.
+template<bool kSorted>
 __global__ __launch_bounds__(kBatchMaxThreads) void
 k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ nodes)
 {
@@ -175,6 +185,8 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
     // ---- 3. stable LSD radix sort of the mesh's codes, 4 x 8 bits ----
     uint32_t* src = b.keys_a + s0;
     uint32_t* dst = b.keys_b + s0;
+    uint32_t* vsrc = kSorted ? b.vals_a + s0 : nullptr; // pass 0 generates the indices
+    uint32_t* vdst = kSorted ? b.vals_b + s0 : nullptr;
     const uint32_t chunk = nthreads * kBatchItems;
     for (uint32_t pass = 0; pass < 4; pass++) {
       const uint32_t shift = pass * 8;
@@ -185,12 +197,14 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
         for (uint32_t k = tid; k < nwarps * 256; k += nthreads)
           s_whist[k] = 0;
         __syncthreads();
-        uint32_t key[kBatchItems], dig[kBatchItems], rank[kBatchItems];
+        uint32_t key[kBatchItems], dig[kBatchItems], rank[kBatchItems], val[kSorted ? kBatchItems : 1];
 #pragma unroll
         for (int k = 0; k < kBatchItems; k++) {
           const uint32_t idx = c0 + warp * (32 * kBatchItems) + uint32_t(k) * 32 + lane;
           key[k] = idx < n ? __ldcg(src + idx) : 0u;
           dig[k] = idx < n ? (key[k] >> shift) & 255u : 256u;
+          if (kSorted)
+            val[kSorted ? k : 0] = idx < n ? (pass == 0 ? idx : __ldcg(vsrc + idx)) : 0u;
         }
         // warp ranking: items in (k, lane) order are in index order
 #pragma unroll
@@ -219,8 +233,12 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < kBatchItems; k++)
-          if (dig[k] < 256)
-            dst[s_run[dig[k]] + s_whist[warp * 256 + dig[k]] + rank[k]] = key[k];
+          if (dig[k] < 256) {
+            const uint32_t at = s_run[dig[k]] + s_whist[warp * 256 + dig[k]] + rank[k];
+            dst[at] = key[k];
+            if (kSorted)
+              vdst[at] = val[kSorted ? k : 0];
+          }
         __syncthreads();
         if (tid < 256)
           s_run[tid] += total;
@@ -229,13 +247,34 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
       uint32_t* t = src;
       src = dst;
       dst = t;
+      if (kSorted) {
+        t = vsrc ? vsrc : b.vals_a + s0;
+        vsrc = vdst;
+        vdst = t;
+      }
     }
-    // four passes: the sorted codes are back in keys_a
+    // four passes: the sorted codes are back in keys_a (the permutation in vals_a)
+    if (kSorted) { // each mesh's triangles in leaf order, for the trace
+      const uint32_t* perm = b.vals_a + s0;
+      const float4* in = reinterpret_cast<const float4*>(tris + s0);
+      float4* out = reinterpret_cast<float4*>(b.sorted_tris + s0);
+      for (uint32_t i = tid; i < n; i += nthreads) {
+        const uint32_t p = __ldcg(perm + i);
+        out[3 * i + 0] = __ldg(in + 3 * p + 0);
+        out[3 * i + 1] = __ldg(in + 3 * p + 1);
+        out[3 * i + 2] = __ldg(in + 3 * p + 2);
+      }
+    }
 
     // ---- 4. bottom-up tree construction (see k_tree_local) ----
     const uint32_t* codes = b.keys_a + s0;
     uint32_t* slots = b.slots + s0;
-    const CgBoxLeaf leaf{ b.boxes + s0 };
+    using TreeLeaf = typename std::conditional<kSorted, CgPermBoxLeaf, CgBoxLeaf>::type;
+    TreeLeaf leaf;
+    if constexpr (kSorted)
+      leaf = CgPermBoxLeaf{ b.boxes + s0, b.vals_a + s0 };
+    else
+      leaf = CgBoxLeaf{ b.boxes + s0 };
     for (uint32_t j = tid; j + 1 < n; j += nthreads)
       slots[j] = kSlotEmpty;
     if (tid == 0)
@@ -327,7 +366,10 @@ launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t
   const uint32_t cap = uint32_t(num_sms) * per_sm;
   const uint32_t grid = b.n_meshes < cap ? b.n_meshes : cap;
   const size_t smem = size_t(threads / 32) * 256 * 4;
-  k_batch_build<<<grid, threads, smem, s>>>(tris, b, nodes);
+  if (b.sorted_tris)
+    k_batch_build<true><<<grid, threads, smem, s>>>(tris, b, nodes);
+  else
+    k_batch_build<false><<<grid, threads, smem, s>>>(tris, b, nodes);
   return cudaGetLastError();
 }
 

@@ -24,8 +24,16 @@ struct BatchBuffers
   Box* boxes;                 // total leaf boxes
   uint32_t* slots;            // total arrival slots (cleared per mesh)
   uint32_t* error;            // sticky kErr* bits
+  // sorted-leaf mode only (nullptr otherwise):
+  uint32_t* vals_a;           // total: the stable sort permutation, per mesh (mesh-local ids)
+  uint32_t* vals_b;           // total
+  Tri* sorted_tris;           // total: each mesh's triangles in leaf (Morton) order
 };
 
+// With b.sorted_tris set, leaf slot p of mesh k holds the p-th triangle of
+// the mesh in stable Morton order (the plain build's sorted-leaf mode, mesh by
+// mesh): the permutation ends in b.vals_a, the reordered triangles in
+// b.sorted_tris.
 cudaError_t launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t threads, int num_sms,
                                cudaStream_t s);
 
@@ -35,9 +43,12 @@ cudaError_t launch_batch_repack(const Node* nodes, uint32_t total_nodes, const u
                                 WideNode* out, cudaStream_t s);
 
 // Rays [roff[m], roff[m + 1]) are traced against mesh m.
+// leaf_prim (sorted-leaf batches): mesh-local triangle id of each leaf slot,
+// indexed like the triangles; nullptr for reference leaf order.
 cudaError_t launch_batch_trace(const WideNode* wnodes,
                                uint32_t total_nodes,
                                const Tri* tris,
+                               const uint32_t* leaf_prim,
                                const uint32_t* off,
                                const uint32_t* roff,
                                uint32_t n_meshes,

@@ -330,7 +330,7 @@ k_trace(const WideNode* __restrict__ wnodes,
     }
     if (!has_cur) {
       Hit h;
-      h.prim = (best_p != kMiss && leaf_prim) ? __ldg(leaf_prim + best_p) : best_p;
+      h.prim = (best_p != kMiss && leaf_prim) ? __ldg(leaf_prim + tb + best_p) : best_p;
       h.t = best_t;
       h.u = best_p != kMiss ? best_u : 0.0f;
       h.v = best_p != kMiss ? best_v : 0.0f;
@@ -591,6 +591,7 @@ cudaError_t
 launch_batch_trace(const WideNode* wnodes,
                    uint32_t total_nodes,
                    const Tri* tris,
+                   const uint32_t* leaf_prim,
                    const uint32_t* off,
                    const uint32_t* roff,
                    uint32_t n_meshes,
@@ -611,7 +612,7 @@ launch_batch_trace(const WideNode* wnodes,
   const uint32_t cap = uint32_t(num_sms) * p.blocks_per_sm;
   const uint32_t blocks = want < cap ? want : cap;
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + total_nodes);
-  k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, nullptr, reinterpret_cast<const float4*>(rays),
+  k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, reinterpret_cast<const float4*>(rays),
                                                         m, hits, nullptr, nullptr, ray_counter, wide, p.refill, off,
                                                         roff, n_meshes);
   return cudaGetLastError();

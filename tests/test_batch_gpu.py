@@ -80,3 +80,28 @@ def test_batch_rejects_bad_offsets(ctx):
         ctx.synchronize()
     ok = lb.Batch(ctx).build(dev(tris), np.array([0, 30, 100], np.uint32))
     assert ok.nodes().size == 98
+
+
+@pytest.mark.parametrize("threads", [256, 1024])
+def test_sorted_leaf_batch_matches_plain_sorted_leaf_builds(ctx, threads):
+    """Sorted-leaf batches: each mesh's node block equals the plain
+    sorted-leaf build of that mesh (itself pinned to the reference builder
+    run on the stably pre-sorted triangles), and the batched trace's hits,
+    with input-order triangle ids, equal the plain sorted-leaf trace's."""
+    ctx.set_param(_lib.PARAM_BATCH_THREADS, threads)
+    try:
+        meshes, tris, off = make_batch([2, 3, 64, 1000, 4097, 30000], 11 + threads)
+        b = lb.Batch(ctx).build(dev(tris), off, sorted_leaves=True)
+        all_nodes = b.nodes()
+        rays, roff, want = [], [0], []
+        for k, m in enumerate(meshes):
+            plain = lb.Builder(ctx, sorted_leaves=True)(m)
+            assert nodes_equal(b.mesh_nodes(k, all_nodes), plain.nodes()), (threads, k)
+            r = scenes.incoherent_rays(m, 500, 40 + k)
+            rays.append(r)
+            roff.append(roff[-1] + r.shape[0])
+            want.append(lb.Traverser(plain)(r))
+        got = lb.hits_view(b.trace(dev(np.concatenate(rays)), dev(np.array(roff, np.uint32).view(np.int32))))
+        assert hit_mismatches(got, np.concatenate(want)).size == 0
+    finally:
+        ctx.set_param(_lib.PARAM_BATCH_THREADS, 512)
