@@ -8,7 +8,7 @@ import pytest
 
 import lbvh_gb300 as lb
 from lbvh_gb300 import scenes
-from conftest import GOLDEN, hit_mismatches, load_golden
+from conftest import nodes_equal, GOLDEN, hit_mismatches, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -68,6 +68,23 @@ def test_config1_torus_primary_and_incoherent(ctx, port):
     want = port.trace(port.build(t, 8), t, rays, 16)
     got = lb.hits_view(lb.Traverser(bvh)(dev(rays)))
     assert_hits_equal(got, want)
+
+
+def test_config2_room_primary_and_diffuse_bounce(ctx, port):
+    # 262,267-triangle clustered room; 1920 x 1080 primary rays from inside
+    # the room and one cosine-weighted diffuse bounce per hit, the bounce rays
+    # made from the oracle's hits so both sides trace the same rays
+    t = scenes.room_scene(seed=21)
+    bvh = lb.Builder(ctx)(dev(t))
+    nodes = port.build(t, 16)
+    assert nodes_equal(bvh.nodes(), nodes)
+    prim = scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))
+    want = port.trace(nodes, t, prim, 16)
+    assert_hits_equal(lb.hits_view(lb.Traverser(bvh)(dev(prim))), want)
+    assert np.mean(want["prim"] != lb.MISS) > 0.5
+    bounce = scenes.diffuse_bounce(prim, want, t, seed=22)
+    want_b = port.trace(nodes, t, bounce, 16)
+    assert_hits_equal(lb.hits_view(lb.Traverser(bvh)(dev(bounce))), want_b)
 
 
 def test_edge_rays_random_soup(ctx, port):
