@@ -121,6 +121,8 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_TRACE_BLOCKS_PER_SM 1 /* persistent traversal grid, 1..32 */
 #define LBVH_PARAM_TRACE_REFILL 2        /* idle lanes before a warp refills, 1..32 */
 #define LBVH_PARAM_BATCH_THREADS 3       /* CTA size of the batched build, 256..1024 */
+#define LBVH_PARAM_TRACE_CHUNK 4         /* rays per chunk of a trace with host rays or hits, whose copies
+                                            then overlap the traversal of other chunks (0: no chunks) */
 LBVH_API int lbvh_ctx_set_param(lbvh_ctx* ctx, int param, int value);
 
 /* Replaces the reference triangle constructor triangle<float>(a, b, c)

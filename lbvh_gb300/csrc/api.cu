@@ -49,6 +49,11 @@ struct lbvh_ctx
   DevBuf prims_in;             // staging for host refit input
   DevBuf roff;                 // staging for host batch ray offsets
   uint32_t* ray_counter = nullptr; // persistent-trace ray dispenser
+  // host-pointer traces in chunks: uploads on copy_in and downloads on
+  // copy_out overlap the traversal on `stream` (made on first use)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_kernel = nullptr, ev_out = nullptr;
+  size_t trace_chunk = size_t(1) << 20; // rays per chunk of a host-pointer trace (0: one piece)
   TraceParams trace;               // traversal launch shape
   uint32_t batch_threads = 512;    // CTA size of the batched build
   DevBuf batch_ws;                 // batched build: codes, boxes, slots
@@ -493,6 +498,14 @@ lbvh_ctx_destroy(lbvh_ctx* c)
   cudaFree(c->state);
   cudaFree(c->ray_counter);
   cudaFreeHost(c->h_err);
+  for (cudaEvent_t e : { c->ev_in, c->ev_kernel, c->ev_out })
+    if (e)
+      cudaEventDestroy(e);
+  for (cudaStream_t q : { c->copy_in, c->copy_out })
+    if (q) {
+      cudaStreamSynchronize(q);
+      cudaStreamDestroy(q);
+    }
   delete c;
   return LBVH_OK;
 }
@@ -552,6 +565,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
       if (value < 1 || value > 32)
         return fail(c, LBVH_ERR_INVALID_ARG, "refill threshold %d outside [1, 32]", value);
       c->trace.refill = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_TRACE_CHUNK:
+      if (value < 0)
+        return fail(c, LBVH_ERR_INVALID_ARG, "trace chunk %d is negative", value);
+      c->trace_chunk = size_t(value);
       return LBVH_OK;
     default:
       return fail(c, LBVH_ERR_INVALID_ARG, "unknown parameter %d", param);
@@ -786,6 +804,20 @@ lbvh_bvh_prepare_trace(lbvh_ctx* c, lbvh_bvh* b)
 }
 
 static int
+ensure_copy_streams(lbvh_ctx* c)
+{
+  if (c->copy_in)
+    return LBVH_OK;
+  CK(cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking), "copy stream");
+  CK(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming), "copy event");
+  CK(cudaEventCreateWithFlags(&c->ev_kernel, cudaEventDisableTiming), "copy event");
+  CK(cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming), "copy event");
+  CK(cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking), "copy stream");
+  return LBVH_OK;
+}
+
+
+int
 trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* hits, uint32_t* n_box, uint32_t* n_tri)
 {
   if (!c || !b || (m && (!rays || !hits)))
@@ -802,13 +834,17 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
   const bool counts = n_box && n_tri;
   const bool hr = !on_device(rays), hh = !on_device(hits);
   const bool hc = counts && (!on_device(n_box) || !on_device(n_tri));
+  // host rays or hits: copies in chunks that overlap the traversal
+  const size_t chunk = c->trace_chunk;
+  const bool pipelined = !counts && (hr || hh) && chunk && m >= 2 * chunk;
   const float* dr = rays;
   Hit* dh = static_cast<Hit*>(hits);
   uint32_t* db = n_box;
   uint32_t* dt = n_tri;
   if (hr) {
     CK(reserve(c->rays, 32 * m, c->stream), "ray staging allocation");
-    CK(cudaMemcpyAsync(c->rays.ptr, rays, 32 * m, cudaMemcpyHostToDevice, c->stream), "ray upload");
+    if (!pipelined)
+      CK(cudaMemcpyAsync(c->rays.ptr, rays, 32 * m, cudaMemcpyHostToDevice, c->stream), "ray upload");
     dr = static_cast<const float*>(c->rays.ptr);
   } else if (reinterpret_cast<uintptr_t>(rays) & 15) {
     return fail(c, LBVH_ERR_INVALID_ARG, "device rays must be 16-byte aligned");
@@ -830,6 +866,35 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
     (b->flags & LBVH_BUILD_SORTED_LEAVES) ? static_cast<const uint32_t*>(b->leaf_prim.ptr) : nullptr;
   if ((st = ensure_wnodes(c, const_cast<lbvh_bvh*>(b))))
     return st;
+  if (pipelined) {
+    if ((st = ensure_copy_streams(c)))
+      return st;
+    // the staging buffers were last used by an earlier call on this context,
+    // which finished before it returned; each chunk has its own region
+    for (size_t o = 0; o < m; o += chunk) {
+      const size_t mc = m - o < chunk ? m - o : chunk;
+      if (hr) {
+        CK(cudaMemcpyAsync(const_cast<float*>(dr) + 8 * o, rays + 8 * o, 32 * mc, cudaMemcpyHostToDevice, c->copy_in),
+           "ray upload");
+        CK(cudaEventRecord(c->ev_in, c->copy_in), "copy event");
+        CK(cudaStreamWaitEvent(c->stream, c->ev_in, 0), "copy wait");
+      }
+      CK(launch_trace_tris(static_cast<const WideNode*>(b->wnodes.ptr), b->n - 1, tris, leaf_prim, dr + 8 * o,
+                           uint32_t(mc), dh + o, nullptr, nullptr, c->ray_counter, c->num_sms, c->trace, c->stream),
+         "trace launch");
+      if (hh) {
+        CK(cudaEventRecord(c->ev_kernel, c->stream), "copy event");
+        CK(cudaStreamWaitEvent(c->copy_out, c->ev_kernel, 0), "copy wait");
+        CK(cudaMemcpyAsync(static_cast<Hit*>(hits) + o, dh + o, 16 * mc, cudaMemcpyDeviceToHost, c->copy_out),
+           "hit download");
+      }
+    }
+    if (hh) {
+      CK(cudaEventRecord(c->ev_out, c->copy_out), "copy event");
+      CK(cudaStreamWaitEvent(c->stream, c->ev_out, 0), "copy wait");
+    }
+    return check_device(c);
+  }
   CK(launch_trace_tris(static_cast<const WideNode*>(b->wnodes.ptr), b->n - 1, tris, leaf_prim, dr, uint32_t(m), dh,
                        counts ? db : nullptr, counts ? dt : nullptr, c->ray_counter, c->num_sms, c->trace,
                        c->stream),

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import lbvh_gb300 as lb
-from lbvh_gb300 import scenes
+from lbvh_gb300 import _lib, scenes
 from conftest import nodes_equal, GOLDEN, hit_mismatches, load_golden
 
 pytestmark = pytest.mark.gpu
@@ -142,3 +142,24 @@ def test_import_rejects_malformed_trees(ctx):
     # the context stays usable
     ok = lb.BVH.from_nodes(g["nodes"], g["tris"], ctx)
     assert_hits_equal(lb.Traverser(ok)(g["rays"]), g["hits"])
+
+
+def test_host_pointer_traces_match_device_traces(ctx):
+    """Traces given host rays and/or host hit buffers go through chunked,
+    overlapped copies once they are large; every combination returns the
+    same hits as the all-device call (sizes straddle the chunking)."""
+    t = scenes.torus_scene(seed=11)
+    bvh = lb.Builder(ctx)(dev(t))
+    ctx.set_param(_lib.PARAM_TRACE_CHUNK, 1 << 18)  # several chunks, with a remainder
+    for m in (1000, (1 << 19) - 1, (1 << 19) + 12345, 1 << 21):
+        rays = scenes.incoherent_rays(t, m, m % 97)
+        ref = lb.hits_view(lb.Traverser(bvh)(dev(rays)))
+        host_host = lb.Traverser(bvh)(rays)
+        pinned = torch.from_numpy(rays).pin_memory()
+        host_dev = lb.hits_view(lb.Traverser(bvh)(pinned, out=torch.empty((m, 4), device="cuda")))
+        dev_host = np.empty(m, lb.HIT_DTYPE)
+        lb.Traverser(bvh)(dev(rays), out=dev_host)
+        ctx.synchronize()
+        for got in (host_host, host_dev, dev_host):
+            assert got.tobytes() == ref.tobytes(), m
+    ctx.set_param(_lib.PARAM_TRACE_CHUNK, 1 << 20)
