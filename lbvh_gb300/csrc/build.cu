@@ -651,6 +651,60 @@ k_tree_global(Leaf leaf,
   }
 }
 
+// The global phase for trees whose n - 1 split positions fit in shared
+// memory: one CTA walks every pending node, with its arrival slots in shared
+// memory and block-scope acquire-release arrivals (a chain of dependent
+// device-scope arrivals costs about a microsecond per tree level; these cost
+// a fraction of that). Records still go to the node array: a record is
+// published by the release half of its writer's next arrival and read after
+// the acquire half of the sibling's, both at block scope.
+template<class Leaf>
+__global__ __launch_bounds__(kTreeGlobalCtaThreads) void
+k_tree_global_cta(Leaf leaf,
+                  uint32_t n,
+                  const uint32_t* __restrict__ codes,
+                  Node* __restrict__ nodes,
+                  const PendingNode* __restrict__ pending_in,
+                  uint32_t pending_cap,
+                  BuildState* __restrict__ st)
+{
+  extern __shared__ uint32_t s_slots[]; // n - 1 split positions
+  for (uint32_t j = threadIdx.x; j + 1 < n; j += blockDim.x)
+    s_slots[j] = kSlotEmpty;
+  __syncthreads();
+  const uint32_t count = min(__ldcg(&st->pending_count), pending_cap);
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    const PendingNode pn = pending_in[i];
+    uint32_t L = pn.L, R = pn.R;
+    Box box = pn.box;
+    bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+    for (uint32_t depth = 0;; depth++) {
+      if (depth > kMaxTreeDepth + 2) {
+        atomicOr(&st->error, kErrBadTopology);
+        break;
+      }
+      const uint32_t s = is_left ? R : L - 1;
+      const uint32_t old = arrive_acq_rel_cta(s_slots + s, is_left ? L : R);
+      if (old == kSlotEmpty)
+        break; // first arrival: the sibling completes the parent
+      const uint32_t LP = is_left ? L : old, RP = is_left ? old : R;
+      const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
+      const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
+      const uint32_t sib = is_left ? cr : cl;
+      const Box other = (sib & kLeafBit) ? leaf(sib & ~kLeafBit) : load_node_box(nodes, sib);
+      box = is_left ? join(box, other) : join(other, box);
+      L = LP;
+      R = RP;
+      if (L == 0 && R == n - 1) {
+        store_node(nodes, 0, box, cl, cr);
+        break;
+      }
+      is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+      store_node(nodes, is_left ? R : L, box, cl, cr);
+    }
+  }
+}
+
 // Parent links from an existing node array (for refit).
 __global__ void
 k_links_from_nodes(const Node* __restrict__ nodes,
@@ -856,6 +910,9 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
   const uint64_t bit = 1ull << (dev & 63);
   if (!(configured.load(std::memory_order_relaxed) & bit)) {
     e = cudaFuncSetAttribute(k_tree_local<Leaf>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTreeSmem));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_tree_global_cta<Leaf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(4 * kTreeGlobalCtaMaxPrims));
     if (e != cudaSuccess)
       return e;
     configured.fetch_or(bit, std::memory_order_relaxed);
@@ -864,6 +921,13 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
   const uint32_t cap = blocks * kTreePendingPerBlock;
   k_tree_local<Leaf><<<blocks, kTreeThreads, kTreeSmem, s>>>(leaf, n, b.keys_a, nodes,
                                                            reinterpret_cast<PendingNode*>(b.pending), cap, b.state);
+  if (blocks == 1)
+    return cudaGetLastError(); // the whole tree was built in the one CTA
+  if (n <= kTreeGlobalCtaMaxPrims) {
+    k_tree_global_cta<Leaf><<<1, kTreeGlobalCtaThreads, size_t(4) * (n - 1), s>>>(
+      leaf, n, b.keys_a, nodes, reinterpret_cast<const PendingNode*>(b.pending), cap, b.state);
+    return cudaGetLastError();
+  }
   k_tree_global<Leaf><<<ceil_div_u32(cap, kFitThreads), kFitThreads, 0, s>>>(
     leaf, n, b.keys_a, b.slots, nodes, reinterpret_cast<const PendingNode*>(b.pending), b.state, epoch);
   return cudaGetLastError();

@@ -22,6 +22,10 @@ constexpr uint32_t kTreeThreads = 256; // threads per CTA of the tree build (4 s
 // dynamic shared memory of the tree build: deltas, slots, node records (each
 // array starts on a 32-byte boundary)
 constexpr size_t kTreeSmem = (kTreeBlock + 8) * 4 + kTreeBlock * 4 + kTreeBlock * 32;
+// Trees of up to this many primitives finish their global phase in one CTA
+// with the arrival slots in shared memory (4 bytes per split position).
+constexpr uint32_t kTreeGlobalCtaMaxPrims = 49152;
+constexpr int kTreeGlobalCtaThreads = 1024;
 static_assert(((kTreeBlock + 8) * 4) % 32 == 0 && (kTreeBlock * 4) % 32 == 0, "smem alignment");
 constexpr uint32_t kSpinLimit = 1u << 22;   // look-back polls before giving up
 constexpr int kLookbackWindow = 8;          // look-back words read per poll
