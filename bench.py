@@ -191,15 +191,22 @@ def run_reference(args, world, rank):
     return 0
 
 
-def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_kind, n=N_BUILD_16M):
+def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_kind, n=N_BUILD_16M, span=1.0):
     """Device-resident build of the 16M-triangle random soup, L2 flushed
-    between builds; the HBM roofline workload."""
+    between builds; the HBM roofline workload. span > 1 (profiling) turns
+    two triangles into points at -span and +span on every axis, so that the
+    soup fills fewer, denser cells of the Morton grid: a smaller soup then
+    has the per-bucket occupancy of the full-size one."""
     import torch
 
     import lbvh_gb300 as lb
     from lbvh_gb300 import scenes
 
-    soup = torch.from_numpy(scenes.soup_large(n, seed=16)).to(dev)
+    host = scenes.soup_large(n, seed=16)
+    if span != 1.0:
+        host[0] = -span
+        host[1] = span
+    soup = torch.from_numpy(host).to(dev)
     big = lb.BVH(ctx)
     ctx.reserve(n, 0)
     for _ in range(3):
@@ -481,6 +488,8 @@ def main():
     ap.add_argument("--no-16m", action="store_true", help="skip the 16M-triangle build measurement")
     ap.add_argument("--only-16m", action="store_true", help="only the 16M-triangle build (profiling)")
     ap.add_argument("--soup-n", type=int, default=N_BUILD_16M, help="soup size of the build measurement")
+    ap.add_argument("--soup-span", type=float, default=1.0,
+                    help="profiling: stretch the soup's bounds to +-span (denser Morton buckets)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
     ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the served-requests measurement")
@@ -523,7 +532,7 @@ def main():
     if args.only_16m:
         flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
         r = measure_build_16m(ctx, lb.Builder(ctx), stream, flush, dev, args.steps, hbm_peak, peak_kind,
-                              args.soup_n)
+                              args.soup_n, args.soup_span)
         if rank == 0:
             print(json.dumps({"build_16m": r}), flush=True)
         return 0

@@ -7,6 +7,7 @@
 #include "build.cuh"
 #include "trace.cuh"
 
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -303,6 +304,18 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
   b.morton_blocks = morton_blocks_for(c, nn);
   const bool keep = flags & LBVH_BUILD_KEEP_CURVE;
   const bool sorted_leaves = flags & LBVH_BUILD_SORTED_LEAVES;
+  b.msd = !keep && !sorted_leaves && nn >= kMsdMinPrims; // keys-only sort of a large build
+  if (b.msd) {
+    // ranges of at least one partition tile, a few per SM; their count rows
+    // (ranges x 16 KB <= 2n + 16 KB) live in vals_a, unused by keys-only sorts
+    const uint32_t want = std::min(uint32_t(c->num_sms) * 8, ceil_div_u32(nn, kPartTile));
+    b.msd_range = (ceil_div_u32(nn, want) + 255u) & ~255u;
+    b.msd_ranges = ceil_div_u32(nn, b.msd_range);
+    // the partition: about two CTAs per SM, each over `group` whole ranges
+    b.msd_group = ceil_div_u32(b.msd_ranges, uint32_t(c->num_sms) * 2);
+    b.sort_ctas = uint32_t(c->num_sms);
+    b.top_rows = b.vals_a;
+  }
 
   if (kind == kKindTris)
     CK(launch_curve_tris(static_cast<const Tri*>(dprims), nn, b, c->stream), "curve launch");

@@ -120,32 +120,43 @@ k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __res
     }
     st->done_counter = 0;
     st->pending_count = 0;
+    st->bucket_next = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++)
       st->tile_counter[k] = 0;
   }
   for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x)
     (&st->hist[0][0])[k] = 0;
+  for (uint32_t k = threadIdx.x; k < kTopBuckets; k += blockDim.x)
+    st->top_hist[k] = 0;
 }
 
 // ---------------------------------------------------------------------------
 // Morton codes (morton_curve_kernel, lbvh.h:1422-1475 with morton_encoder<4>,
 // lbvh.h:1345-1359): q = u32((center - min) * scale), code = x<<2 | y<<1 | z.
 // Also accumulates the four 8-bit digit histograms the radix sort needs, so
-// the sort never re-reads the codes just to count them.
-
-template<class Leaf>
+// the sort never re-reads the codes just to count them. With kTop (the bucket
+// sort of large keys-only builds) CTA b takes the codes [b * range, +range)
+// and also writes their counts per bucket of the top 12 bits to row b of
+// `rows`.
+template<class Leaf, bool kTop>
 __global__ __launch_bounds__(kMortonThreads) void
-k_morton(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes, BuildState* __restrict__ st)
+k_morton(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes, BuildState* __restrict__ st, uint32_t range,
+         uint32_t* __restrict__ rows)
 {
   __shared__ uint32_t s_hist[4 * 256];
+  __shared__ uint32_t s_top[kTop ? kTopBuckets : 1]; // buckets of the top 12 bits, for the bucket sort
   for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x)
     s_hist[k] = 0;
+  if (kTop)
+    for (uint32_t k = threadIdx.x; k < kTopBuckets; k += blockDim.x)
+      s_top[k] = 0;
   __syncthreads();
   const float lo0 = st->lo[0], lo1 = st->lo[1], lo2 = st->lo[2];
   const float s0 = st->scale[0], s1 = st->scale[1], s2 = st->scale[2];
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  const uint32_t stride = kTop ? blockDim.x : gridDim.x * blockDim.x;
+  const uint32_t end = kTop ? (n - blockIdx.x * range < range ? n : blockIdx.x * range + range) : n;
+  for (uint32_t i = (kTop ? blockIdx.x * range : blockIdx.x * blockDim.x) + threadIdx.x; i < end; i += stride) {
     const Box bx = leaf(i);
     const float cx = fmul(fadd(bx.lo[0], bx.hi[0]), 0.5f);
     const float cy = fmul(fadd(bx.lo[1], bx.hi[1]), 0.5f);
@@ -159,8 +170,17 @@ k_morton(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes, BuildState* __rest
     atomicAdd(&s_hist[1 * 256 + ((code >> 8) & 255u)], 1u);
     atomicAdd(&s_hist[2 * 256 + ((code >> 16) & 255u)], 1u);
     atomicAdd(&s_hist[3 * 256 + (code >> 24)], 1u);
+    if (kTop)
+      atomicAdd(&s_top[code >> (30 - kTopBits)], 1u); // codes are 30 bits
   }
   __syncthreads();
+  if (kTop)
+    for (uint32_t k = threadIdx.x; k < kTopBuckets; k += blockDim.x) {
+      const uint32_t c = s_top[k];
+      rows[size_t(blockIdx.x) * kTopBuckets + k] = c;
+      if (c)
+        atomicAdd(&st->top_hist[k], c);
+    }
   for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) {
     const uint32_t c = s_hist[k];
     if (c)
@@ -242,8 +262,11 @@ k_onesweep(const uint32_t* __restrict__ kin,
            uint32_t pass,
            uint32_t epoch,
            unsigned long long* __restrict__ lookback,
-           BuildState* __restrict__ st)
+           BuildState* __restrict__ st,
+           bool skip_if_msd)
 {
+  if (skip_if_msd && st->use_msd)
+    return; // the bucket sort did this build's sorting
   __shared__ uint32_t s_keys[kSortTile];
   __shared__ uint32_t s_vals[kPairs ? kSortTile : 1];
   __shared__ uint32_t s_whist[kSortWarps][256];
@@ -390,6 +413,436 @@ k_onesweep(const uint32_t* __restrict__ kin,
       if (kPairs)
         vout[o] = s_vals[i];
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Keys-only sort of large builds by buckets. Only the sorted code sequence
+// reaches the tree (leaf p is primitive p), so equal codes may land in any
+// order. The codes are partitioned by their top 12 bits into 4,096 buckets,
+// then each bucket is sorted by its low 18 bits in shared memory by one CTA.
+//
+//   k_morton (kTop)  one CTA per range of `range` consecutive codes: writes
+//                    the range's bucket counts as one row of `rows`
+//                    [ranges][4096] and adds them to st->top_hist;
+//   k_top_scan       bucket starts (st->top_base), the choice of path, and
+//                    each range's start in each bucket (column prefix sums of
+//                    `rows`, in place);
+//   k_partition      one CTA per range: places its codes at those starts
+//                    (shared-memory atomics rank the codes of a tile, so no
+//                    global atomics);
+//   k_bucket_sort    one CTA per bucket: an unstable pass by bits 0-8 into
+//                    shared memory, then a stable pass by bits 9-17 into the
+//                    output; the first pass may be unstable because codes
+//                    equal in all 30 bits are interchangeable.
+//
+// k_top_scan chooses this path when every bucket holds at most kBucketMax
+// codes, the four onesweep passes otherwise; both are launched and the
+// unchosen kernels return at once, so the choice needs no host read-back.
+
+// Exclusive scan of one value per thread over a block of kWarps warps.
+template<int kWarps>
+__device__ __forceinline__ uint32_t
+block_excl_scan(uint32_t v, uint32_t* s_warp)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o)
+      x += y;
+  }
+  if (lane == 31)
+    s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < kWarps ? s_warp[lane] : 0u;
+    uint32_t t = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o)
+        t += y;
+    }
+    if (lane < kWarps)
+      s_warp[lane] = t - w;
+  }
+  __syncthreads();
+  const uint32_t r = x - v + s_warp[warp];
+  __syncthreads();
+  return r;
+}
+
+// kTopBuckets / 32 CTAs of 1,024 threads; CTA b owns buckets [32b, 32b + 32)
+// (lane = bucket): warp w sums its block of rows, the warps' sums are
+// scanned through shared memory, and warp w rewrites its rows as starts.
+// Every access to `rows` is one 128-byte line per warp.
+__global__ __launch_bounds__(1024) void
+k_top_scan(uint32_t* __restrict__ rows, uint32_t nrows, BuildState* __restrict__ st)
+{
+  constexpr int kPer = kTopBuckets / 1024;
+  constexpr uint32_t kBatch = 8;
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_max;
+  __shared__ uint32_t s_base[kTopBuckets];
+  __shared__ uint32_t s_part[32][33];
+  const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t == 0)
+    s_max = 0;
+  __syncthreads();
+  // every CTA scans the bucket totals (16 KB); CTA 0 publishes them
+  uint32_t c[kPer], sum = 0, mx = 0;
+#pragma unroll
+  for (int j = 0; j < kPer; j++) {
+    c[j] = st->top_hist[kPer * t + j];
+    sum += c[j];
+    mx = max(mx, c[j]);
+  }
+  atomicMax(&s_max, mx);
+  uint32_t ex = block_excl_scan<32>(sum, s_warp);
+#pragma unroll
+  for (int j = 0; j < kPer; j++) {
+    s_base[kPer * t + j] = ex;
+    if (blockIdx.x == 0)
+      st->top_base[kPer * t + j] = ex;
+    ex += c[j];
+  }
+  const bool use = s_max <= kBucketMax;
+  if (blockIdx.x == 0) {
+    if (t == 1023)
+      st->top_base[kTopBuckets] = ex; // == n
+    if (t == 0)
+      st->use_msd = use ? 1u : 0u;
+    // the non-empty buckets in ascending order, for the bucket sort's CTAs
+    uint32_t nz = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; j++)
+      nz += c[j] != 0;
+    uint32_t at = block_excl_scan<32>(nz, s_warp);
+#pragma unroll
+    for (int j = 0; j < kPer; j++)
+      if (c[j] != 0)
+        st->top_list[at++] = kPer * t + j;
+    if (t == 1023)
+      st->top_nonempty = at;
+  }
+  if (!use)
+    return; // uniform over the CTA
+  const uint32_t d = blockIdx.x * 32 + lane;
+  const uint32_t per = (nrows + 31) / 32;
+  const uint32_t r_lo = min(nrows, warp * per);
+  const uint32_t r_hi = min(nrows, r_lo + per);
+  uint32_t part = 0;
+#pragma unroll 1
+  for (uint32_t r0 = r_lo; r0 < r_hi; r0 += kBatch) {
+    uint32_t v[kBatch];
+#pragma unroll
+    for (uint32_t u = 0; u < kBatch; u++)
+      v[u] = r0 + u < r_hi ? rows[size_t(r0 + u) * kTopBuckets + d] : 0u;
+#pragma unroll
+    for (uint32_t u = 0; u < kBatch; u++)
+      part += v[u];
+  }
+  s_part[warp][lane] = part;
+  __syncthreads();
+  uint32_t run = s_base[d];
+  for (uint32_t w = 0; w < warp; w++)
+    run += s_part[w][lane];
+#pragma unroll 1
+  for (uint32_t r0 = r_lo; r0 < r_hi; r0 += kBatch) {
+    uint32_t v[kBatch];
+#pragma unroll
+    for (uint32_t u = 0; u < kBatch; u++)
+      v[u] = r0 + u < r_hi ? rows[size_t(r0 + u) * kTopBuckets + d] : 0u;
+#pragma unroll
+    for (uint32_t u = 0; u < kBatch; u++)
+      if (r0 + u < r_hi) {
+        rows[size_t(r0 + u) * kTopBuckets + d] = run;
+        run += v[u];
+      }
+  }
+}
+
+// One CTA per range [blockIdx.x * range, +range) of the unsorted codes
+// (`group` consecutive ranges of the Morton pass, so its starts are the
+// first of their rows), in tiles of kPartTile: each tile's codes are ranked within their bucket by
+// shared-memory atomics, grouped by bucket in shared memory and written at
+// the range's running position in each bucket (runs of consecutive codes).
+// Tiles arrive by cp.async into two shared buffers: the next tile is in
+// flight while the current one is ranked, and a tile's buffer then holds its
+// regrouped codes.
+__global__ __launch_bounds__(kPartThreads) void
+k_partition(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout, uint32_t n, uint32_t range,
+            uint32_t group, const uint32_t* __restrict__ rows, const BuildState* __restrict__ st)
+{
+  if (!st->use_msd)
+    return;
+  constexpr int kPer = kTopBuckets / kPartThreads; // buckets per thread in the scans
+  constexpr uint32_t kChunks = kPartTile / 4 / kPartThreads; // 16-byte copies per thread per tile
+  extern __shared__ __align__(16) uint32_t smem_p[];
+  uint32_t* s_cur = smem_p;                   // [kTopBuckets] the range's next output position per bucket
+  uint32_t* s_start = s_cur + kTopBuckets;    // [kTopBuckets] counts, then the tile's bucket starts
+  uint32_t* s_stage = s_start + kTopBuckets;  // [2][kPartTile] tiles as loaded, then regrouped
+  __shared__ uint32_t s_warp[32];
+  const uint32_t tid = threadIdx.x;
+  const uint32_t lo = blockIdx.x * range;     // a multiple of 256 codes: 16-byte aligned
+  const uint32_t hi = n - lo < range ? n : lo + range;
+  // tile `base` -> s_stage[buf]; a copy past hi reads only the codes below hi
+  auto fetch = [&](uint32_t base, uint32_t buf) {
+#pragma unroll
+    for (uint32_t j = 0; j < kChunks; j++) {
+      const uint32_t c = j * kPartThreads + tid; // 16-byte chunk within the tile
+      const uint32_t i = base + 4 * c;
+      const uint32_t bytes = i < hi ? min(16u, 4 * (hi - i)) : 0u;
+      copy16_async(s_stage + buf * kPartTile + 4 * c, bytes ? kin + i : kin, bytes);
+    }
+  };
+  for (uint32_t k = tid; k < kTopBuckets; k += kPartThreads)
+    s_cur[k] = rows[size_t(blockIdx.x) * group * kTopBuckets + k]; // the range's first row
+  fetch(lo, 0);
+  copy_async_commit();
+  uint32_t buf = 0;
+#pragma unroll 1
+  for (uint32_t base = lo; base < hi; base += kPartTile, buf ^= 1u) {
+    if (base + kPartTile < hi)
+      fetch(base + kPartTile, buf ^ 1u);
+    copy_async_commit();
+    for (uint32_t k = tid; k < kTopBuckets; k += kPartThreads)
+      s_start[k] = 0;
+    copy_async_wait<1>(); // this tile's copies (all but the newest group)
+    __syncthreads();
+    uint32_t* tile = s_stage + buf * kPartTile;
+    uint32_t key[kPartItems], pk[kPartItems]; // pk: rank in the tile's bucket << 12 | bucket
+#pragma unroll
+    for (int k = 0; k < kPartItems; k++)
+      key[k] = tile[uint32_t(k) * kPartThreads + tid];
+#pragma unroll
+    for (int k = 0; k < kPartItems; k++) {
+      const uint32_t idx = base + uint32_t(k) * kPartThreads + tid;
+      pk[k] = 0xffffffffu;
+      if (idx < hi) {
+        const uint32_t d = key[k] >> (30 - kTopBits); // codes are 30 bits
+        pk[k] = (atomicAdd(&s_start[d], 1u) << kTopBits) | d;
+      }
+    }
+    __syncthreads();
+    uint32_t c[kPer], sum = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+      c[j] = s_start[kPer * tid + j];
+      sum += c[j];
+    }
+    uint32_t ex = block_excl_scan<kPartThreads / 32>(sum, s_warp);
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+      s_start[kPer * tid + j] = ex;
+      ex += c[j];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kPartItems; k++)
+      if (pk[k] != 0xffffffffu)
+        tile[s_start[pk[k] & (kTopBuckets - 1)] + (pk[k] >> kTopBits)] = key[k];
+    __syncthreads();
+    const uint32_t tile_n = min(uint32_t(kPartTile), hi - base);
+    for (uint32_t i = tid; i < tile_n; i += kPartThreads) {
+      const uint32_t k = tile[i];
+      const uint32_t d = k >> (30 - kTopBits);
+      kout[s_cur[d] + (i - s_start[d])] = k;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kPer; j++)
+      s_cur[kPer * tid + j] += c[j];
+  }
+  copy_async_wait<0>();
+}
+
+// Persistent CTAs of 1,024 threads (one per SM) take the non-empty buckets
+// from st->top_list in turn. Per bucket: the codes are read once (into
+// shared buffer A, counted on the way); an unstable counting pass by bits
+// 0-12 (shared-memory atomics) scatters them into shared buffer B; a stable pass by bits 13-17 ranks them
+// per warp (one ballot per digit bit, up to kBucketChunk codes per step,
+// spread evenly over the warps) into shared buffer A, which is written out
+// in order.
+__global__ __launch_bounds__(kBucketThreads, 1) void
+k_bucket_sort(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout, BuildState* __restrict__ st)
+{
+  if (!st->use_msd)
+    return;
+  constexpr int kWarps = kBucketThreads / 32;
+  constexpr uint32_t kPerThread = kBucketMax / kBucketThreads;
+  constexpr int kFirstPer = kFirstDigits / kBucketThreads;
+  constexpr uint32_t kFirstMask = kFirstDigits - 1, kSecondMask = kSecondDigits - 1;
+  constexpr uint32_t kInvalid = 0xffffffffu; // codes are 30 bits
+  static_assert(kBucketMax % kBucketThreads == 0, "whole codes per thread");
+  static_assert(kFirstDigits % kBucketThreads == 0, "whole first-pass digits per thread");
+  static_assert(kSecondDigits == kWarps, "one second-pass digit per warp in the offset scan");
+  static_assert(kFirstBits + kSecondBits == 30 - kTopBits, "the passes cover the bits below the bucket");
+  extern __shared__ __align__(16) uint32_t smem_b[];
+  uint32_t* A = smem_b;                                                     // [kBucketMax]
+  uint32_t* B = A + kBucketMax;                                             // [kBucketMax]
+  uint32_t* s_first = B + kBucketMax;                                       // [kFirstDigits]
+  uint32_t* s_run = s_first + kFirstDigits;                                 // [kSecondDigits]
+  uint16_t* whist = reinterpret_cast<uint16_t*>(s_run + kSecondDigits);     // [kWarps][kSecondDigits]
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_take;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t buckets = st->top_nonempty;
+
+#pragma unroll 1
+  for (;;) {
+    if (tid == 0)
+      s_take = atomicAdd(&st->bucket_next, 1u);
+    __syncthreads();
+    const uint32_t take = s_take;
+    if (take >= buckets)
+      break; // uniform over the CTA
+    const uint32_t bkt = st->top_list[take];
+    const uint32_t cnt = st->top_hist[bkt]; // <= kBucketMax when use_msd is set
+    const uint32_t start = st->top_base[bkt];
+    const uint32_t* src = kin + start;
+
+#pragma unroll
+    for (int j = 0; j < kFirstPer; j++)
+      s_first[kFirstPer * tid + j] = 0;
+    if (tid < kSecondDigits)
+      s_run[tid] = 0;
+    uint32_t v[kPerThread];
+#pragma unroll
+    for (uint32_t u = 0; u < kPerThread; u++) {
+      const uint32_t i = u * kBucketThreads + tid;
+      v[u] = i < cnt ? __ldcs(src + i) : kInvalid;
+    }
+    __syncthreads(); // also: every thread has read s_take
+#pragma unroll
+    for (uint32_t u = 0; u < kPerThread; u++)
+      if (u * kBucketThreads < cnt && v[u] != kInvalid) {
+        A[u * kBucketThreads + tid] = v[u];
+        atomicAdd(&s_first[v[u] & kFirstMask], 1u);
+        atomicAdd(&s_run[(v[u] >> kFirstBits) & kSecondMask], 1u);
+      }
+    __syncthreads();
+    {
+      uint32_t sum = 0;
+#pragma unroll
+      for (int j = 0; j < kFirstPer; j++)
+        sum += s_first[kFirstPer * tid + j];
+      // warp 0 scans the second-pass histogram (one digit per lane) meanwhile
+      uint32_t h = 0, hx = 0;
+      if (warp == 0) {
+        h = s_run[lane];
+        uint32_t x = h;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o)
+            x += y;
+        }
+        hx = x - h;
+      }
+      uint32_t ex = block_excl_scan<kWarps>(sum, s_warp);
+#pragma unroll
+      for (int j = 0; j < kFirstPer; j++) {
+        const uint32_t cj = s_first[kFirstPer * tid + j]; // this thread's own digits
+        s_first[kFirstPer * tid + j] = ex;
+        ex += cj;
+      }
+      if (warp == 0)
+        s_run[lane] = hx;
+    }
+    __syncthreads();
+    // unstable pass by bits 0-12: A -> B
+#pragma unroll 4
+    for (uint32_t i = tid; i < cnt; i += kBucketThreads) {
+      const uint32_t k = A[i];
+      B[atomicAdd(&s_first[k & kFirstMask], 1u)] = k;
+    }
+    __syncthreads();
+    // stable pass by bits 13-17: B -> A
+#pragma unroll 1
+    for (uint32_t c0 = 0; c0 < cnt; ) {
+      const uint32_t ipw = min(uint32_t(kBucketItems), (cnt - c0 + kBucketThreads - 1) / kBucketThreads);
+      const uint32_t step = ipw * kBucketThreads;
+      const bool full = c0 + step <= cnt;
+      if (tid < kWarps * kSecondDigits / 2)
+        reinterpret_cast<uint32_t*>(whist)[tid] = 0;
+      __syncthreads();
+      const uint32_t first = c0 + warp * ipw * 32 + lane;
+      uint32_t key[kBucketItems], rank[kBucketItems];
+      // the lanes holding the same digit, for every item first (independent
+      // ballots), then the items' counts in order through the warp's histogram
+#pragma unroll
+      for (int k = 0; k < kBucketItems; k++) {
+        if (uint32_t(k) < ipw) {
+          const uint32_t idx = first + uint32_t(k) * 32;
+          key[k] = (full || idx < cnt) ? B[idx] : kInvalid;
+          const uint32_t d = (key[k] >> kFirstBits) & kSecondMask; // invalid: matches no valid lane
+          uint32_t peers = full ? 0xffffffffu : __ballot_sync(0xffffffffu, key[k] != kInvalid);
+#pragma unroll
+          for (uint32_t b = 0; b < kSecondBits; b++) {
+            const uint32_t bit = (d >> b) & 1u;
+            const uint32_t m = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? m : ~m;
+          }
+          rank[k] = peers;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kBucketItems; k++) {
+        if (uint32_t(k) < ipw) {
+          const bool valid = key[k] != kInvalid;
+          const uint32_t d = (key[k] >> kFirstBits) & kSecondMask;
+          const uint32_t peers = rank[k];
+          const uint32_t pre = __popc(peers & lt_mask);
+          uint32_t before = 0;
+          if (valid)
+            before = whist[warp * kSecondDigits + d];
+          __syncwarp();
+          if (valid && pre == 0)
+            whist[warp * kSecondDigits + d] = uint16_t(before + __popc(peers));
+          __syncwarp();
+          rank[k] = before + pre;
+        }
+      }
+      __syncthreads();
+      // per digit, exclusive offsets over the warps: warp w scans digit w
+      // with lane = the warp whose count it holds
+      uint32_t tot;
+      {
+        const uint32_t i0 = lane * kSecondDigits + warp;
+        const uint32_t cw = whist[i0];
+        uint32_t x = cw;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o)
+            x += y;
+        }
+        whist[i0] = uint16_t(x - cw);
+        tot = __shfl_sync(0xffffffffu, x, 31);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kBucketItems; k++) {
+        if (uint32_t(k) < ipw && key[k] != kInvalid) {
+          const uint32_t d = (key[k] >> kFirstBits) & kSecondMask;
+          A[s_run[d] + whist[warp * kSecondDigits + d] + rank[k]] = key[k];
+        }
+      }
+      __syncthreads();
+      if (lane == 0)
+        s_run[warp] += tot;
+      c0 += step;
+    }
+    __syncthreads();
+    uint32_t* dst = kout + start;
+    for (uint32_t i = tid; i < cnt; i += kBucketThreads)
+      dst[i] = A[i];
+    // the next bucket's first writes to s_first / s_run / B / A all follow
+    // at least one more barrier; A is read here, written after three
   }
 }
 
@@ -865,16 +1318,50 @@ launch_curve(const Leaf& leaf, uint32_t n, const BuildBuffers& b, cudaStream_t s
 {
   k_bounds<Leaf><<<b.bounds_blocks, kBoundsThreads, 0, s>>>(leaf, n, reinterpret_cast<ArgBox*>(b.partials), b.state,
                                                             stage);
-  if (stage)
-    k_morton<BoxLeaf><<<b.morton_blocks, kMortonThreads, 0, s>>>(BoxLeaf{ stage }, n, b.keys_a, b.state);
-  else
-    k_morton<Leaf><<<b.morton_blocks, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state);
+  if (stage) {
+    if (b.msd)
+      k_morton<BoxLeaf, true><<<b.msd_ranges, kMortonThreads, 0, s>>>(BoxLeaf{ stage }, n, b.keys_a, b.state,
+                                                                      b.msd_range, b.top_rows);
+    else
+      k_morton<BoxLeaf, false><<<b.morton_blocks, kMortonThreads, 0, s>>>(BoxLeaf{ stage }, n, b.keys_a, b.state, 0,
+                                                                          nullptr);
+  } else {
+    if (b.msd)
+      k_morton<Leaf, true><<<b.msd_ranges, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state, b.msd_range,
+                                                                   b.top_rows);
+    else
+      k_morton<Leaf, false><<<b.morton_blocks, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state, 0, nullptr);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t
 launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s)
 {
+  const bool msd = b.msd && !pairs;
+  if (msd) {
+    static std::atomic<uint64_t> configured{ 0 }; // the shared-memory opt-in, once per device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+      return e;
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(configured.load(std::memory_order_relaxed) & bit)) {
+      e = cudaFuncSetAttribute(k_bucket_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBucketSmem));
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_partition, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPartSmem));
+      if (e != cudaSuccess)
+        return e;
+      configured.fetch_or(bit, std::memory_order_relaxed);
+    }
+    // the bucket sort (keys_a -> keys_b -> keys_a), or nothing if a bucket is too large
+    k_top_scan<<<kTopBuckets / 32, 1024, 0, s>>>(b.top_rows, b.msd_ranges, b.state);
+    const uint32_t ctas = ceil_div_u32(b.msd_ranges, b.msd_group);
+    k_partition<<<ctas, kPartThreads, kPartSmem, s>>>(b.keys_a, b.keys_b, n, b.msd_range * b.msd_group,
+                                                      b.msd_group, b.top_rows, b.state);
+    k_bucket_sort<<<b.sort_ctas, kBucketThreads, kBucketSmem, s>>>(b.keys_b, b.keys_a, b.state);
+  }
+  // the onesweep passes (they return at once when the bucket sort ran)
   const uint32_t tiles = ceil_div_u32(n, kSortTile);
   uint32_t* ka = b.keys_a;
   uint32_t* kb = b.keys_b;
@@ -884,11 +1371,14 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
     const uint32_t epoch = epoch_base + pass;
     if (pairs) {
       if (pass == 0)
-        k_onesweep<true, true><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, vb, n, pass, epoch, b.lookback, b.state);
+        k_onesweep<true, true><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, vb, n, pass, epoch, b.lookback, b.state,
+                                                             false);
       else
-        k_onesweep<true, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, va, vb, n, pass, epoch, b.lookback, b.state);
+        k_onesweep<true, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, va, vb, n, pass, epoch, b.lookback, b.state,
+                                                              false);
     } else {
-      k_onesweep<false, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass, epoch, b.lookback, b.state);
+      k_onesweep<false, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass, epoch, b.lookback,
+                                                             b.state, msd);
     }
     std::swap(ka, kb);
     std::swap(va, vb);

@@ -13,6 +13,23 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems; // 4096 keys per tile
+// Keys-only sort of large builds: partition by the top 12 code bits, then
+// sort each bucket by its low 18 bits in shared memory (used when every
+// bucket fits).
+constexpr uint32_t kMsdMinPrims = 1u << 18;   // smaller builds use the onesweep passes only
+constexpr int kTopBits = 12, kTopBuckets = 1 << kTopBits;
+// the bucket sort's two passes over the low 18 bits: an unstable one by bits
+// 0-12, a stable one by bits 13-17
+constexpr int kFirstBits = 13, kFirstDigits = 1 << kFirstBits;
+constexpr int kSecondBits = 5, kSecondDigits = 1 << kSecondBits;
+constexpr int kPartThreads = 512, kPartItems = 16;
+constexpr int kPartTile = kPartThreads * kPartItems; // 8192 keys per partition tile
+constexpr size_t kPartSmem = (size_t(2) * kTopBuckets + 2 * size_t(kPartTile)) * 4;
+constexpr int kBucketThreads = 1024, kBucketItems = 8;
+constexpr int kBucketChunk = kBucketThreads * kBucketItems; // 8192 keys ranked per step
+constexpr uint32_t kBucketMax = 20480;          // largest bucket sorted in shared memory
+constexpr size_t kBucketSmem = size_t(2) * kBucketMax * 4 + size_t(kBucketThreads / 32) * kSecondDigits * 2 +
+                               size_t(kFirstDigits + kSecondDigits) * 4;
 constexpr int kFitThreads = 256;
 constexpr uint32_t kTreeBlock = 1024; // leaf slots per CTA of the tree build
 // Pending-list capacity per CTA: the canonical pieces of a slot range number
@@ -68,6 +85,12 @@ struct BuildBuffers
   Box* boxes;                     // optional: leaf boxes staged by the bounds pass (n)
   uint32_t bounds_blocks;
   uint32_t morton_blocks;
+  bool msd;                       // keys-only build large enough for the bucket sort (kMsdMinPrims)
+  uint32_t msd_range;             // bucket sort: codes per range (a multiple of 256)
+  uint32_t msd_ranges;            // bucket sort: ranges = CTAs of the Morton pass
+  uint32_t msd_group;             // bucket sort: ranges per CTA of the partition
+  uint32_t sort_ctas;             // bucket sort: persistent CTAs (one per SM)
+  uint32_t* top_rows;             // bucket sort: msd_ranges x kTopBuckets counts (in vals_a)
 };
 
 cudaError_t launch_make_triangles(const float* verts, uint32_t n, Tri* out, cudaStream_t s);

@@ -60,6 +60,13 @@ struct BuildState
   uint32_t pending_count;      // tree build: nodes left for the global phase
   uint32_t error;              // sticky kErr* bits
   uint32_t pad1;
+  // keys-only sort by buckets of the top 12 code bits (see k_top_scan)
+  uint32_t top_hist[4096];     // histogram of code >> 18
+  uint32_t top_base[4097];     // bucket starts (exclusive scan), top_base[4096] = n
+  uint32_t use_msd;            // 1: the bucket sort runs; 0: the four onesweep passes run
+  uint32_t top_nonempty;       // number of non-empty buckets
+  uint32_t bucket_next;        // bucket sort: next entry of top_list to take
+  uint32_t top_list[4096];     // the non-empty buckets, ascending
 };
 
 // ---- exact scalar ops --------------------------------------------------

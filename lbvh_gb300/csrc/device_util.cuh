@@ -163,4 +163,27 @@ stage_record(Node& rec, const Box& b, uint32_t l, uint32_t r)
   rec.right = r;
 }
 
+// Asynchronous 16-byte copy global -> shared (cp.async, L2 only); bytes
+// beyond src_bytes (0..16) are zero-filled and not read.
+__device__ __forceinline__ void
+copy16_async(void* smem, const void* gmem, uint32_t src_bytes)
+{
+  const uint32_t s = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+
+__device__ __forceinline__ void
+copy_async_commit()
+{
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// Waits until at most kPending of this thread's committed groups are in flight.
+template<int kPending>
+__device__ __forceinline__ void
+copy_async_wait()
+{
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kPending) : "memory");
+}
+
 } // namespace lbvh_gb300
