@@ -123,6 +123,11 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_BATCH_THREADS 3       /* CTA size of the batched build, 256..1024 */
 #define LBVH_PARAM_TRACE_CHUNK 4         /* rays per chunk of a trace with host rays or hits, whose copies
                                             then overlap the traversal of other chunks (0: no chunks) */
+#define LBVH_PARAM_TRACE_IN_PLACE 5      /* host rays / hits in page-locked (pinned) memory: 0 copies them,
+                                            1 reads the rays in place, 2 (default) also writes the hits in
+                                            place, each warp's batch of 32 as one 512-byte store (the
+                                            traversal then reaches host memory over the CPU-GPU link);
+                                            pageable host memory is always copied */
 LBVH_API int lbvh_ctx_set_param(lbvh_ctx* ctx, int param, int value);
 
 /* Replaces the reference triangle constructor triangle<float>(a, b, c)

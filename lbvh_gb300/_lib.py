@@ -29,6 +29,7 @@ PARAM_TRACE_BLOCKS_PER_SM = 1
 PARAM_TRACE_REFILL = 2
 PARAM_BATCH_THREADS = 3
 PARAM_TRACE_CHUNK = 4
+PARAM_TRACE_IN_PLACE = 5
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000

@@ -55,6 +55,7 @@ struct lbvh_ctx
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
   cudaEvent_t ev_in = nullptr, ev_kernel = nullptr, ev_out = nullptr;
   size_t trace_chunk = size_t(1) << 20; // rays per chunk of a host-pointer trace (0: one piece)
+  int trace_in_place = 2;               // LBVH_PARAM_TRACE_IN_PLACE
   TraceParams trace;               // traversal launch shape
   uint32_t batch_threads = 512;    // CTA size of the batched build
   DevBuf batch_ws;                 // batched build: codes, boxes, slots
@@ -119,6 +120,19 @@ on_device(const void* p)
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// The device address of page-locked host memory (cudaHostAlloc'd or
+// registered), or null for anything else.
+void*
+mapped_host(const void* p)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 // Grow-only stream-ordered buffer.
@@ -584,6 +598,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "trace chunk %d is negative", value);
       c->trace_chunk = size_t(value);
       return LBVH_OK;
+    case LBVH_PARAM_TRACE_IN_PLACE:
+      if (value < 0 || value > 2)
+        return fail(c, LBVH_ERR_INVALID_ARG, "trace in-place mode %d outside [0, 2]", value);
+      c->trace_in_place = value;
+      return LBVH_OK;
     default:
       return fail(c, LBVH_ERR_INVALID_ARG, "unknown parameter %d", param);
   }
@@ -845,8 +864,24 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
   if (st)
     return st;
   const bool counts = n_box && n_tri;
-  const bool hr = !on_device(rays), hh = !on_device(hits);
+  bool hr = !on_device(rays), hh = !on_device(hits);
   const bool hc = counts && (!on_device(n_box) || !on_device(n_tri));
+  const bool host_io = hr || hh || hc; // results in host memory: finish before returning
+  // page-locked host rays / hits the traversal reaches in place
+  if (hr && c->trace_in_place >= 1) {
+    if (const void* d = mapped_host(rays)) {
+      rays = static_cast<const float*>(d);
+      hr = false;
+    }
+  }
+  bool hits_in_place = false;
+  if (hh && c->trace_in_place >= 2) {
+    if (void* d = mapped_host(hits)) {
+      hits = d;
+      hh = false;
+      hits_in_place = true;
+    }
+  }
   // host rays or hits: copies in chunks that overlap the traversal
   const size_t chunk = c->trace_chunk;
   const bool pipelined = !counts && (hr || hh) && chunk && m >= 2 * chunk;
@@ -910,7 +945,7 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
   }
   CK(launch_trace_tris(static_cast<const WideNode*>(b->wnodes.ptr), b->n - 1, tris, leaf_prim, dr, uint32_t(m), dh,
                        counts ? db : nullptr, counts ? dt : nullptr, c->ray_counter, c->num_sms, c->trace,
-                       c->stream),
+                       c->stream, hits_in_place && !counts),
      "trace launch");
   if (hh)
     CK(cudaMemcpyAsync(hits, dh, 16 * m, cudaMemcpyDeviceToHost, c->stream), "hit download");
@@ -918,7 +953,7 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
     CK(cudaMemcpyAsync(n_box, db, 4 * m, cudaMemcpyDefault, c->stream), "count download");
     CK(cudaMemcpyAsync(n_tri, dt, 4 * m, cudaMemcpyDefault, c->stream), "count download");
   }
-  if (hr || hh || hc)
+  if (host_io)
     return check_device(c);
   return LBVH_OK;
 }

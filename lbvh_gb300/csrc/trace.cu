@@ -160,8 +160,18 @@ k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict_
 
 // kBatch: rays [roff[k], roff[k + 1]) belong to mesh k, whose nodes start at
 // moff[k] - k and whose triangles start at moff[k] (local indices inside).
-template<bool kCounts, bool kBatch>
-__global__ __launch_bounds__(kTraceThreads) void
+//
+// kHostHits: `hits` is page-locked host memory reached over the CPU-GPU
+// link, where 16-byte stores scattered in time travel one by one. Each warp
+// then keeps the hits of its last kHitRing ray batches (32 consecutive rays
+// each) in shared memory and writes a batch out with one 512-byte store of
+// the warp once its last ray has finished; a batch that finds its ring entry
+// still taken by an unfinished older batch writes its hits directly.
+constexpr uint32_t kHitRing = 4;
+constexpr uint32_t kHitDirect = kHitRing; // a ray whose hit is written directly
+
+template<bool kCounts, bool kBatch, bool kHostHits = false>
+__global__ __launch_bounds__(kTraceThreads, 8) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
         const uint32_t* __restrict__ leaf_prim,
@@ -201,7 +211,43 @@ k_trace(const WideNode* __restrict__ wnodes,
   uint32_t batch = 0, batch_left = 0;
   bool no_more = false; // the last batch fetched reached the end of the rays
 
+  // kHostHits: per warp, kHitRing staged batches {hits, first ray, rays left}
+  constexpr int kWarps = kTraceThreads / 32;
+  __shared__ Hit s_hits[kHostHits ? kWarps : 1][kHostHits ? kHitRing : 1][32];
+  __shared__ uint32_t s_first[kHostHits ? kWarps : 1][kHostHits ? kHitRing : 1];
+  __shared__ uint32_t s_left[kHostHits ? kWarps : 1][kHostHits ? kHitRing : 1];
+  const uint32_t wid = threadIdx.x >> 5;
+  uint32_t seq = 0;             // batches this warp has fetched
+  uint32_t batch_buf = kHitDirect; // ring entry of the current batch
+  uint32_t buf = kHitDirect;    // ring entry of this lane's ray
+  bool flush = false;           // this lane finished the last ray of its batch
+  if (kHostHits) {
+    if (lane < kHitRing)
+      s_left[wid][lane] = 0;
+    __syncwarp();
+  }
+
   for (;;) {
+    if (kHostHits) {
+      // ---- write out the batches whose last ray finished (whole warp) ----
+      uint32_t fl = __ballot_sync(0xffffffffu, flush);
+      if (fl) {
+        __syncwarp(); // the staged hits of every lane are visible
+        while (fl) {
+          const uint32_t src = __ffs(fl) - 1;
+          fl &= fl - 1;
+          const uint32_t b = __shfl_sync(0xffffffffu, buf, src);
+          const uint32_t first = s_first[wid][b];
+          if (first + lane < m)
+            hits[first + lane] = s_hits[wid][b][lane];
+        }
+        __syncwarp(); // every read of the ring entries before they are reused
+        if (flush) {
+          buf = kHitDirect;
+          flush = false;
+        }
+      }
+    }
     // ---- refill idle lanes from the warp's batch (ballot + shuffle) ----
     const uint32_t idle = __ballot_sync(0xffffffffu, ray == kMiss);
     if (__popc(idle) >= refill) { // warp-uniform; refill <= 32
@@ -216,6 +262,7 @@ k_trace(const WideNode* __restrict__ wnodes,
         batch_left -= got;
         uint32_t extra_base = 0;
         bool fetched = false;
+        const uint32_t old_buf = batch_buf;
         if (got < want && !no_more) {
           uint32_t nb = 0;
           if (lane == 0)
@@ -226,16 +273,36 @@ k_trace(const WideNode* __restrict__ wnodes,
           batch = nb;
           batch_left = 32 - (want - got);
           fetched = true;
+          if (kHostHits && nb < m) {
+            // the ring entry of this batch, unless an older batch still holds it
+            const uint32_t k = seq % kHitRing;
+            seq++;
+            batch_buf = kHitDirect;
+            if (s_left[wid][k] == 0) {
+              batch_buf = k;
+              __syncwarp();
+              if (lane == 0) {
+                s_first[wid][k] = nb;
+                s_left[wid][k] = min(32u, m - nb);
+              }
+              __syncwarp();
+            }
+          }
         }
         if (ray == kMiss) {
           const uint32_t k = __popc(idle & lt_mask);
           uint32_t id = kMiss;
-          if (k < got)
+          uint32_t id_buf = old_buf;
+          if (k < got) {
             id = next_id + k;
-          else if (fetched)
+          } else if (fetched) {
             id = extra_base + (k - got);
+            id_buf = batch_buf;
+          }
           if (id < m) {
             ray = id;
+            if (kHostHits)
+              buf = id_buf;
             r = make_ray(__ldg(rays + 2 * size_t(id)), __ldg(rays + 2 * size_t(id) + 1));
             r.fast = r.fast && scene_fast;
           if (kBatch) { // the mesh k with roff[k] <= id < roff[k + 1]
@@ -334,7 +401,12 @@ k_trace(const WideNode* __restrict__ wnodes,
       h.t = best_t;
       h.u = best_p != kMiss ? best_u : 0.0f;
       h.v = best_p != kMiss ? best_v : 0.0f;
-      hits[ray] = h;
+      if (kHostHits && buf != kHitDirect) {
+        s_hits[wid][buf][ray - s_first[wid][buf]] = h;
+        flush = atomicSub(&s_left[wid][buf], 1u) == 1u; // the batch's last ray
+      } else {
+        hits[ray] = h;
+      }
       if (kCounts) {
         n_box[ray] = cb;
         n_tri[ray] = ct;
@@ -369,7 +441,8 @@ launch_trace_tris(const WideNode* wnodes,
                   uint32_t* ray_counter,
                   int num_sms,
                   const TraceParams& p,
-                  cudaStream_t s)
+                  cudaStream_t s,
+                  bool host_hits)
 {
   if (m == 0)
     return cudaSuccess;
@@ -385,6 +458,10 @@ launch_trace_tris(const WideNode* wnodes,
   if (n_box && n_tri)
     k_trace<true, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri,
                                                           ray_counter, wide, p.refill, nullptr, nullptr, 0);
+  else if (host_hits)
+    k_trace<false, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
+                                                                 nullptr, ray_counter, wide, p.refill, nullptr,
+                                                                 nullptr, 0);
   else
     k_trace<false, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
                                                            ray_counter, wide, p.refill, nullptr, nullptr, 0);

@@ -40,7 +40,8 @@ cudaError_t launch_trace_tris(const WideNode* wnodes,
                               uint32_t* ray_counter,
                               int num_sms,
                               const TraceParams& p,
-                              cudaStream_t s);
+                              cudaStream_t s,
+                              bool host_hits = false); // hits: page-locked host memory
 
 // Hit record of the sphere intersector: {prim, t, uv, normal, pad}, 32 bytes.
 struct __align__(16) SphereHit

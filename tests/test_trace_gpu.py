@@ -163,3 +163,30 @@ def test_host_pointer_traces_match_device_traces(ctx):
         for got in (host_host, host_dev, dev_host):
             assert got.tobytes() == ref.tobytes(), m
     ctx.set_param(_lib.PARAM_TRACE_CHUNK, 1 << 20)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_pinned_traces_in_place_match_device_traces(ctx, mode):
+    """Page-locked host rays and hit buffers are copied (mode 0), or the
+    rays are read in place (1) and the hits written in place too (2, each
+    warp writing its batches of 32 hits from shared memory); every mode and
+    mix returns the device call's hits, for counts that are not multiples of
+    32 and ones that span many batches per warp."""
+    t = scenes.torus_scene(seed=11)
+    bvh = lb.Builder(ctx)(dev(t))
+    ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, mode)
+    try:
+        for m in (1, 1000, 12345, (1 << 20) + 7):
+            rays = scenes.incoherent_rays(t, m, m % 89)
+            ref = lb.hits_view(lb.Traverser(bvh)(dev(rays))).tobytes()
+            rays_p = torch.from_numpy(rays).pin_memory()
+            hits_p = torch.empty((m, 4), dtype=torch.float32).pin_memory()
+            lb.Traverser(bvh)(rays_p, out=hits_p)
+            assert lb.hits_view(hits_p).tobytes() == ref, (mode, m)
+            hits_p.fill_(-1.0)
+            lb.Traverser(bvh)(dev(rays), out=hits_p)  # device rays, pinned hits
+            assert lb.hits_view(hits_p).tobytes() == ref, (mode, m)
+            got = lb.Traverser(bvh)(rays_p, out=torch.empty((m, 4), device="cuda"))  # pinned rays, device hits
+            assert lb.hits_view(got).tobytes() == ref, (mode, m)
+    finally:
+        ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, 2)
