@@ -867,16 +867,19 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
   bool hr = !on_device(rays), hh = !on_device(hits);
   const bool hc = counts && (!on_device(n_box) || !on_device(n_tri));
   const bool host_io = hr || hh || hc; // results in host memory: finish before returning
-  // page-locked host rays / hits the traversal reaches in place
+  // page-locked host rays / hits the traversal reaches in place (16-byte
+  // aligned ones; others are copied like pageable memory)
   if (hr && c->trace_in_place >= 1) {
-    if (const void* d = mapped_host(rays)) {
+    const void* d = mapped_host(rays);
+    if (d && !(reinterpret_cast<uintptr_t>(d) & 15)) {
       rays = static_cast<const float*>(d);
       hr = false;
     }
   }
   bool hits_in_place = false;
   if (hh && c->trace_in_place >= 2) {
-    if (void* d = mapped_host(hits)) {
+    void* d = mapped_host(hits);
+    if (d && !(reinterpret_cast<uintptr_t>(d) & 15)) {
       hits = d;
       hh = false;
       hits_in_place = true;

@@ -188,5 +188,14 @@ def test_pinned_traces_in_place_match_device_traces(ctx, mode):
             assert lb.hits_view(hits_p).tobytes() == ref, (mode, m)
             got = lb.Traverser(bvh)(rays_p, out=torch.empty((m, 4), device="cuda"))  # pinned rays, device hits
             assert lb.hits_view(got).tobytes() == ref, (mode, m)
+        # pinned buffers that are not 16-byte aligned are copied instead
+        m = 4097
+        rays = scenes.incoherent_rays(t, m, 5)
+        ref = lb.hits_view(lb.Traverser(bvh)(dev(rays))).tobytes()
+        rays_p = torch.empty(8 * m + 1, dtype=torch.float32).pin_memory()
+        rays_p[1:] = torch.from_numpy(rays.reshape(-1))
+        hits_p = torch.empty(4 * m + 1, dtype=torch.float32).pin_memory()
+        lb.Traverser(bvh)(rays_p[1:].view(m, 8), out=hits_p[1:].view(m, 4))
+        assert lb.hits_view(hits_p[1:].view(m, 4)).tobytes() == ref, mode
     finally:
         ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, 2)
