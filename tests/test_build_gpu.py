@@ -45,7 +45,7 @@ def test_build_matches_golden(ctx, name):
         assert nodes_equal(b.nodes(), g["user_box_nodes"])
 
 
-@pytest.mark.parametrize("n", [2, 3, 31, 1000, 4095, 4096, 4097, 8193, 65537, 300_007])
+@pytest.mark.parametrize("n", [2, 3, 31, 1000, 4095, 4096, 4097, 8193, 20480, 20481, 65537, 300_007])
 def test_build_matches_oracle_random(ctx, port, n):
     t = scenes.soup(n, seed=n)
     bvh = lb.Builder(ctx, keep_curve=True)(dev(t))
@@ -58,6 +58,8 @@ def test_build_matches_oracle_random(ctx, port, n):
     ref_nodes = port.build(t, 8)
     assert nodes_equal(bvh.nodes(), ref_nodes)
     assert port.check_bvh(bvh.nodes()) == 0
+    # keys-only sort (one-CTA sort up to 20,480 codes, onesweep passes above)
+    assert nodes_equal(lb.Builder(ctx)(dev(t)).nodes(), ref_nodes)
     sl = lb.Builder(ctx, sorted_leaves=True)(dev(t))
     assert nodes_equal(sl.nodes(), port.build(t[perm], 8))
 
