@@ -191,7 +191,7 @@ morton_blocks_for(const lbvh_ctx* c, uint32_t n)
 int
 ws_reserve(lbvh_ctx* c, size_t n)
 {
-  const size_t tiles = (n + kSortTile - 1) / kSortTile;
+  const size_t tiles = sort_tiles(n);
   const size_t A = 256;
   size_t off = 0;
   auto take = [&](size_t bytes) {

@@ -252,7 +252,7 @@ block_excl_scan_256(uint32_t v, uint32_t* s_warp)
   return r;
 }
 
-template<bool kPairs, bool kIotaVals>
+template<bool kPairs, bool kIotaVals, int kItems = kSortItems>
 __global__ __launch_bounds__(kSortThreads, kPairs ? 3 : 4) void
 k_onesweep(const uint32_t* __restrict__ kin,
            uint32_t* __restrict__ kout,
@@ -265,10 +265,11 @@ k_onesweep(const uint32_t* __restrict__ kin,
            BuildState* __restrict__ st,
            bool skip_if_msd)
 {
+  constexpr int kTile = kSortThreads * kItems;
   if (skip_if_msd && st->use_msd)
     return; // the bucket sort did this build's sorting
-  __shared__ uint32_t s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kPairs ? kSortTile : 1];
+  __shared__ uint32_t s_keys[kTile];
+  __shared__ uint32_t s_vals[kPairs ? kTile : 1];
   __shared__ uint32_t s_whist[kSortWarps][256];
   __shared__ uint32_t s_tile_start[256];
   __shared__ uint32_t s_gbase[256];
@@ -282,17 +283,17 @@ k_onesweep(const uint32_t* __restrict__ kin,
     (&s_whist[0][0])[i] = 0;
   __syncthreads();
   const uint32_t tile = s_tile;
-  const uint32_t base = tile * uint32_t(kSortTile);
+  const uint32_t base = tile * uint32_t(kTile);
   const uint32_t shift = pass * 8;
 
   // digits are recomputed from the keys where needed (fewer live registers)
-  const uint32_t first = base + uint32_t(warp) * (32 * kSortItems) + lane;
+  const uint32_t first = base + uint32_t(warp) * (32 * kItems) + lane;
   auto digit = [&](uint32_t kv, int k) -> uint32_t {
     return first + uint32_t(k) * 32 < n ? (kv >> shift) & 255u : 256u; // 256: not a key, in no bucket
   };
-  uint32_t key[kSortItems], val[kPairs ? kSortItems : 1], rank[kSortItems];
+  uint32_t key[kItems], val[kPairs ? kItems : 1], rank[kItems];
 #pragma unroll
-  for (int k = 0; k < kSortItems; k++) {
+  for (int k = 0; k < kItems; k++) {
     const uint32_t idx = first + uint32_t(k) * 32;
     key[k] = idx < n ? kin[idx] : 0u;
     if (kPairs)
@@ -306,9 +307,9 @@ k_onesweep(const uint32_t* __restrict__ kin,
   // non-keys.
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t digit_bits = pass == 3 ? 6u : 8u; // codes are 30 bits
-  const bool full_tile = base + uint32_t(kSortTile) <= n;
+  const bool full_tile = base + uint32_t(kTile) <= n;
 #pragma unroll
-  for (int k = 0; k < kSortItems; k++) {
+  for (int k = 0; k < kItems; k++) {
     const uint32_t d = digit(key[k], k);
     uint32_t peers = full_tile ? 0xffffffffu : __ballot_sync(0xffffffffu, d < 256);
 #pragma unroll
@@ -391,7 +392,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
 
   // reorder the tile in shared memory by digit
 #pragma unroll
-  for (int k = 0; k < kSortItems; k++) {
+  for (int k = 0; k < kItems; k++) {
     const uint32_t d = digit(key[k], k);
     if (d < 256) {
       const uint32_t pos = s_tile_start[d] + s_whist[warp][d] + rank[k];
@@ -403,7 +404,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
   __syncthreads();
 
   // write out: consecutive positions of one digit go to consecutive addresses
-  const uint32_t tile_n = min(uint32_t(kSortTile), n - base);
+  const uint32_t tile_n = min(uint32_t(kTile), n - base);
   for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
     const uint32_t k = s_keys[i];
     const uint32_t d = (k >> shift) & 255u;
@@ -1361,8 +1362,10 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
                                                       b.msd_group, b.top_rows, b.state);
     k_bucket_sort<<<b.sort_ctas, kBucketThreads, kBucketSmem, s>>>(b.keys_b, b.keys_a, b.state);
   }
-  // the onesweep passes (they return at once when the bucket sort ran)
-  const uint32_t tiles = ceil_div_u32(n, kSortTile);
+  // the onesweep passes (they return at once when the bucket sort ran);
+  // small keys-only sorts use smaller tiles, so that more SMs take part
+  const bool small = !pairs && n <= kSmallTileMaxPrims;
+  const uint32_t tiles = ceil_div_u32(n, small ? kSmallTile : kSortTile);
   uint32_t* ka = b.keys_a;
   uint32_t* kb = b.keys_b;
   uint32_t* va = b.vals_a;
@@ -1376,6 +1379,9 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
       else
         k_onesweep<true, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, va, vb, n, pass, epoch, b.lookback, b.state,
                                                               false);
+    } else if (small) {
+      k_onesweep<false, false, kSmallTileItems><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass,
+                                                                              epoch, b.lookback, b.state, msd);
     } else {
       k_onesweep<false, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass, epoch, b.lookback,
                                                              b.state, msd);

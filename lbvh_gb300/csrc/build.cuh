@@ -13,6 +13,15 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = 16;
 constexpr int kSortTile = kSortThreads * kSortItems; // 4096 keys per tile
+// keys-only sorts of at most kSmallTileMaxPrims codes: tiles of kSmallTile
+constexpr int kSmallTileItems = 4;
+constexpr int kSmallTile = kSortThreads * kSmallTileItems; // 1024 keys per tile
+constexpr uint32_t kSmallTileMaxPrims = 65536;
+// look-back words a sort of n codes needs (tiles x 256)
+constexpr size_t sort_tiles(size_t n)
+{
+  return n <= kSmallTileMaxPrims ? (n + kSmallTile - 1) / kSmallTile : (n + kSortTile - 1) / kSortTile;
+}
 // Keys-only sort of large builds: partition by the top 12 code bits, then
 // sort each bucket by its low 18 bits in shared memory (used when every
 // bucket fits).

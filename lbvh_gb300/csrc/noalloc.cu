@@ -41,7 +41,7 @@ round_up(size_t x)
   return (x + kAlign - 1) / kAlign * kAlign;
 }
 
-constexpr size_t kTiles = (kNoAllocMaxPrims + kSortTile - 1) / kSortTile;
+constexpr size_t kTiles = sort_tiles(kNoAllocMaxPrims);
 constexpr size_t kBoundsBlocksMax = (kNoAllocMaxPrims + kBoundsThreads * 8 - 1) / (kBoundsThreads * 8);
 // scratch layout (byte offsets)
 constexpr size_t kOffState = 0;
