@@ -281,7 +281,7 @@ LBVH_API int lbvh_batch_trace_triangles(lbvh_ctx* ctx, const lbvh_batch* batch, 
  * device node array of (n - 1) x 32 bytes (32-byte aligned); the result is
  * bit-identical to lbvh_build_triangles with flags 0. All other memory is a
  * fixed scratch array inside the library, sized for LBVH_NOALLOC_MAX_PRIMS
- * primitives (about 1.4 MB, held by every GPU that loads the library until
+ * primitives (about 1.5 MB, held by every GPU that loads the library until
  * the process exits); larger n is rejected with LBVH_ERR_INVALID_ARG, as are
  * host pointers. The call allocates nothing and does not synchronize: work
  * is queued on `stream` (a cudaStream_t, NULL = default stream) on the

@@ -10,7 +10,7 @@
 // array; everything else the build needs lives in one file-scope device array
 // below.
 //
-// The scratch array is fixed at kNoAllocMaxPrims primitives (about 1.4 MB).
+// The scratch array is fixed at kNoAllocMaxPrims primitives (about 1.5 MB).
 // Every GPU that loads this library reserves it until the process exits.
 // All calls on a device share it and it keeps the last call's contents, so
 // each call clears the parts that must start at zero (the build counters and
