@@ -42,7 +42,7 @@ constexpr size_t kTriBytes = 48, kRayBytes = 32, kHitBytes = 16, kNodeBytes = 32
 size_t
 scene_bytes(size_t n)
 {
-  return 144 * n + (size_t(1) << 16); // triangles 48 + nodes 32 + traversal copy 64, per triangle
+  return 148 * n + (size_t(1) << 16); // triangles 48 + nodes 32 + traversal copy 64 + sorted codes 4, per triangle
 }
 
 struct Request

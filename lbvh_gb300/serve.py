@@ -70,8 +70,8 @@ class Request:
 
 def scene_bytes(n: int) -> int:
     """Device bytes a resident scene of n triangles holds: triangles (48),
-    nodes (32), traversal copy (64) per triangle."""
-    return 144 * n + (1 << 16)
+    nodes (32), traversal copy (64), sorted codes (4) per triangle."""
+    return 148 * n + (1 << 16)
 
 
 def _exception(status: int, msg: str) -> BaseException:

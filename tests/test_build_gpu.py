@@ -112,6 +112,33 @@ def test_refit_matches_oracle(ctx, port, sorted_leaves):
     # host-side refit input as well
     bvh.refit(t2)
     assert nodes_equal(bvh.nodes(), want)
+    # a refit after another build on the same context (the codes are the BVH's own)
+    lb.Builder(ctx)(dev(scenes.soup(50_000, 5)))
+    bvh.refit(dev(t))
+    want0 = port.build(t[perm], 8) if sorted_leaves else port.build(t, 8)
+    assert nodes_equal(bvh.nodes(), want0)
+    if not sorted_leaves:
+        # a tree given as a node array has no codes: the refit walks its links
+        loaded = lb.BVH.from_nodes(want0, t, ctx)
+        loaded.refit(dev(t2))
+        assert nodes_equal(loaded.nodes(), want)
+
+
+@pytest.mark.parametrize("n", [300_000, 600_000, 2_000_000])
+def test_large_refit_matches_oracle(ctx, port, n):
+    """Refits of at least 2^19 primitives rerun the tree phase over the
+    build's own sorted codes (smaller ones walk the node links); either way
+    the result equals the oracle's topology-preserving fit."""
+    t = scenes.soup(n, 41) if n <= 600_000 else scenes.soup_large(n, seed=41)
+    bvh = lb.Builder(ctx)(dev(t))
+    t2 = (t + np.float32(0.01)).astype(np.float32)
+    bvh.refit(dev(t2))
+    assert nodes_equal(bvh.nodes(), port.refit(port.build(t, 16), t2))
+    if n == 600_000:  # sorted-leaf mode: the moved triangles are gathered into leaf order first
+        sl = lb.Builder(ctx, sorted_leaves=True)(dev(t))
+        sl.refit(dev(t2))
+        perm = port.curve(t, 16)[2]
+        assert nodes_equal(sl.nodes(), port.refit(port.build(t[perm], 16), t2[perm]))
 
 
 def test_invalid_arguments_raise(ctx):
