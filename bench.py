@@ -191,7 +191,8 @@ def run_reference(args, world, rank):
     return 0
 
 
-def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_kind, n=N_BUILD_16M, span=1.0):
+def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_kind, n=N_BUILD_16M, span=1.0,
+                      with_refit=False):
     """Device-resident build of the 16M-triangle random soup, L2 flushed
     between builds; the HBM roofline workload. span > 1 (profiling) turns
     two triangles into points at -span and +span on every axis, so that the
@@ -223,10 +224,27 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
         bt.append(a.elapsed_time(b))
     ctx.synchronize()
     ms16 = float(np.mean(bt))
+    refit_ms = None
+    if with_refit:  # the same tree over moved triangles (topology kept)
+        moved = soup + 0.001
+        big.refit(moved)
+        torch.cuda.synchronize()
+        rt = []
+        for _ in range(max(5, min(steps, 20))):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            big.refit(moved)
+            b.record(stream)
+            torch.cuda.synchronize()
+            rt.append(a.elapsed_time(b))
+        refit_ms = round(float(np.mean(rt)), 4)
+        del moved
     algo = n * sum(BYTES_PER_PRIM.values())
     achieved = algo / (ms16 * 1e-3) / 1e9
     return {"triangles": n, "ms": round(ms16, 4),
             "mprims_s": round(n / (ms16 * 1e-3) / 1e6, 1),
+            "refit_ms": refit_ms,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "bytes_per_prim": sum(BYTES_PER_PRIM.values()),
@@ -635,7 +653,7 @@ def main():
     if not args.no_16m:
         del tris_p, rays_p, hits_p
         build_16m = measure_build_16m(ctx, builder, stream, flush, dev, args.steps, hbm_peak, peak_kind,
-                                      args.soup_n)
+                                      args.soup_n, with_refit=True)
 
     # ---- batched meshes (4,096 soups) vs the plain per-mesh path ----------
     batched = None
