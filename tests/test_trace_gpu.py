@@ -113,6 +113,39 @@ def test_edge_rays_random_soup(ctx, port):
     assert_hits_equal(lb.Traverser(bvh)(r), port.trace(nodes, t, r, 8))
 
 
+def test_extreme_coordinates_and_directions(ctx, port):
+    """Box coordinates beyond 2^60 switch the traversal to the reference's
+    exact ternary min/max (the fast fminf/fmaxf slab path needs every slab
+    value finite), and so do rays with a direction component below 2^-60 in
+    magnitude; hits stay bit-identical."""
+    t = scenes.soup(3000, seed=12)
+    far = scenes.soup(8, seed=13) * np.float32(1e30)  # a few triangles far out
+    t = np.concatenate([t, far]).astype(np.float32)
+    nodes = port.build(t, 8)
+    bvh = lb.Builder(ctx)(dev(t))
+    assert nodes_equal(bvh.nodes(), nodes)
+    rays = scenes.incoherent_rays(t[:3000], 20_000, 14)
+    rays[::7, 3] = np.float32(1e-30)   # nearly axis-parallel rays
+    rays[1::11, 4] = np.float32(-0.0)
+    rays[2::13, 0:3] *= np.float32(1e25)  # origins far out
+    assert_hits_equal(lb.hits_view(lb.Traverser(bvh)(dev(rays))), port.trace(nodes, t, rays, 8))
+
+
+def test_signed_zero_ties_in_boxes(ctx, port):
+    """Triangles whose vertex coordinates are +0.0 and -0.0 in turn: every
+    min/max tie between the two zeros resolves as the reference's folds do
+    (bounds, leaf boxes, node boxes compared bit for bit)."""
+    rng = np.random.default_rng(15)
+    v = rng.uniform(-1, 1, (4000, 9)).astype(np.float32)
+    zero = rng.random(v.shape) < 0.3
+    v[zero] = np.where(rng.random(zero.sum()) < 0.5, np.float32(0.0), np.float32(-0.0))
+    t = scenes.make_triangles(v)
+    bvh = lb.Builder(ctx, keep_curve=True)(dev(t))
+    assert nodes_equal(bvh.nodes(), port.build(t, 8))
+    assert nodes_equal(lb.Builder(ctx)(dev(t)).nodes(), port.build(t, 8))
+    assert np.array_equal(bvh.curve()[3].view(np.uint32), port.centroid_bounds(t, 8).view(np.uint32))
+
+
 def test_user_box_bvh_has_no_triangle_traverser(ctx):
     b = lb.Builder(ctx)(np.zeros((4, 6), np.float32), converter=lb.BOXES)
     with pytest.raises(ValueError):
