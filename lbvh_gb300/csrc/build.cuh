@@ -25,7 +25,7 @@ constexpr size_t sort_tiles(size_t n)
 // Keys-only sort of large builds: partition by the top 12 code bits, then
 // sort each bucket by its low 18 bits in shared memory (used when every
 // bucket fits).
-constexpr uint32_t kMsdMinPrims = 1u << 18;   // smaller builds use the onesweep passes only
+constexpr uint32_t kMsdMinPrims = 1500000; // smaller builds use the onesweep passes only (faster below ~1.5M)
 constexpr int kTopBits = 12, kTopBuckets = 1 << kTopBits;
 // the bucket sort's two passes over the low 18 bits: an unstable one by bits
 // 0-12, a stable one by bits 13-17

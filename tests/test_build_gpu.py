@@ -187,25 +187,24 @@ def test_dump_and_reload_round_trip(lib_built, tmp_path):
         lb.BVH.load(tmp_path / "bad.npz")
 
 
-@pytest.mark.parametrize("kind", ["uniform", "dense_bucket", "crowded", "all_equal"])
+@pytest.mark.parametrize("kind", ["uniform", "dense_bucket", "over_bucket", "crowded", "all_equal"])
 def test_large_builds_with_crowded_buckets_match_oracle(ctx, port, kind):
-    """Large keys-only builds sort by buckets of the top 12 code bits when
-    every bucket holds at most 20,480 codes and by the radix passes
-    otherwise. A uniform soup and one with a bucket filled close to that
-    limit by 20,000 equal codes take the first path; a scene whose codes
-    crowd one bucket, and one whose codes are all equal, take the second.
-    All match the oracle."""
-    n = 300_000
-    if kind == "uniform":
-        t = scenes.soup(n, seed=90)
-    elif kind == "dense_bucket":
-        t = scenes.soup(n, seed=93)
-        t[:20_000] = t[0]
+    """Keys-only builds of at least 1.5M primitives sort by buckets of the
+    top 12 code bits when every bucket holds at most 20,480 codes and by the
+    radix passes otherwise. A uniform soup and one with a bucket filled to
+    19,543 codes (18,000 of them equal) take the first path; 1,000 more
+    equal codes (20,542 in the bucket), a scene whose codes crowd one bucket,
+    and one whose codes are all equal take the second. All match the
+    oracle."""
+    n = 1_600_000
+    if kind in ("uniform", "dense_bucket", "over_bucket"):
+        t = scenes.soup_large(n, seed=90)
+        if kind != "uniform":
+            t[: 18_000 if kind == "dense_bucket" else 19_000] = t[0]
     elif kind == "crowded":
-        v = scenes.soup_vertices(n, 91) * 1e-3   # a tight cluster at the origin...
-        v[:2000] *= 1e3                          # ...and a few triangles spread wide
-        t = scenes.make_triangles(v)
+        t = scenes.soup_large(n, seed=91) * np.float32(1e-3)  # a tight cluster at the origin...
+        t[:2000] *= np.float32(1e3)                           # ...and a few triangles spread wide
     else:
-        t = scenes.make_triangles(np.tile(scenes.soup_vertices(1, 92), (n, 1)))
+        t = np.tile(scenes.soup_large(1, seed=92), (n, 1))
     bvh = lb.Builder(ctx)(dev(t))
-    assert nodes_equal(bvh.nodes(), port.build(t, 8))
+    assert nodes_equal(bvh.nodes(), port.build(t, 16))
