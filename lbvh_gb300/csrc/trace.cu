@@ -349,7 +349,8 @@ k_trace(const WideNode* __restrict__ wnodes,
         rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
       }
       // leaf triangles, left before right (equal t: the first tested wins)
-#pragma unroll 1
+      if ((left | right) & kLeafBit)
+#pragma unroll
       for (int k = 0; k < 2; k++) {
         const uint32_t c = k == 0 ? left : right;
         if (c & kLeafBit) {
