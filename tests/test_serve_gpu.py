@@ -120,3 +120,30 @@ def test_evicted_scenes_are_dumped_and_reloaded(lib_built):
     assert hit_mismatches(got1, want1).size == 0
     assert hit_mismatches(got3, want3[1][0]).size == 0
     assert hit_mismatches(got3b, want3[3][0]).size == 0
+
+
+def test_page_locked_request_buffers(lib_built):
+    """Requests whose triangles, rays and hit buffers are page-locked host
+    memory (pinned tensors' storage, and cudaHostRegister'd numpy arrays)
+    give the plain path's results."""
+    t = scenes.soup(20_000, 61)
+    rays = scenes.incoherent_rays(t, 50_000, 62)
+    want = run_plain([(0.0, "build", 0, t), (0.0, "trace", 0, rays)])[1][0]
+    pinned_t = torch.from_numpy(t).pin_memory()
+    pinned_r = torch.from_numpy(rays).pin_memory()
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32).pin_memory()
+    reg = np.ascontiguousarray(rays.copy())
+    reg_hits = np.empty(rays.shape[0], lb.HIT_DTYPE)
+    cudart = torch.cuda.cudart()
+    for a in (reg, reg_hits):
+        assert int(getattr(r := cudart.cudaHostRegister(a.ctypes.data, a.nbytes, 0), "value", r)) == 0
+    try:
+        with Server(slots=2) as srv:
+            srv.submit("build", 0, pinned_t.numpy()).result(timeout=120)
+            got = srv.submit("trace", 0, pinned_r.numpy(), out=hits.numpy().view(lb.HIT_DTYPE).reshape(-1)).result(timeout=120)
+            assert hit_mismatches(got, want).size == 0
+            got = srv.submit("trace", 0, reg, out=reg_hits).result(timeout=120)
+            assert hit_mismatches(got, want).size == 0
+    finally:
+        for a in (reg, reg_hits):
+            cudart.cudaHostUnregister(a.ctypes.data)
