@@ -260,14 +260,73 @@ def _pct(xs, q):
 SERVE_SLOTS = 16  # worker streams of the request server
 
 
-def _result_buffers(reqs, device):
+class _PinnedArena:
+    """One page-locked host allocation that request arrays and hit buffers
+    are carved from (256-byte aligned), as a serving front end's pooled I/O
+    buffers are."""
+
+    def __init__(self, nbytes):
+        import torch
+
+        self._t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, pin_memory=True)
+        self._a = self._t.numpy()
+        self._off = 0
+
+    def take(self, nbytes):
+        assert self._off + nbytes <= self._a.shape[0]
+        v = self._a[self._off : self._off + nbytes]
+        self._off += (nbytes + 255) & ~255
+        return v
+
+
+def _owner(a):
+    while isinstance(a.base, np.ndarray):
+        a = a.base
+    return a
+
+
+def _pinned_requests(reqs):
+    """The same requests with every data array moved into one page-locked
+    arena (views keep their offsets within a shared array, so ray slices of
+    one pooled ray set stay slices of one pinned copy), and room for both
+    paths' hit buffers. Returns (arena, requests)."""
+    owners = {}
+    for _, _, _, d in reqs:
+        o = _owner(d)
+        assert o.flags.c_contiguous and d.flags.c_contiguous
+        owners.setdefault(id(o), o)
+    hit_bytes = sum(d.shape[0] * 16 for _, k, _, d in reqs if k == "trace")
+    size = sum((o.nbytes + 255) & ~255 for o in owners.values()) + 2 * (hit_bytes + 256 * len(reqs))
+    arena = _PinnedArena(size)
+    copies = {}
+    for key, o in owners.items():
+        p = arena.take(o.nbytes)
+        p[:] = o.reshape(-1).view(np.uint8)
+        copies[key] = (o, p)
+    out, views = [], {}
+    for at, kind, scene, d in reqs:
+        if id(d) not in views:
+            o, p = copies[id(_owner(d))]
+            off = d.__array_interface__["data"][0] - o.__array_interface__["data"][0]
+            views[id(d)] = p[off : off + d.nbytes].view(d.dtype).reshape(d.shape)
+        out.append((at, kind, scene, views[id(d)]))
+    return arena, out
+
+
+def _result_buffers(reqs, device, arena=None):
     """One hit buffer per trace request, already mapped for device copies
-    (as a serving front end's pooled response buffers are)."""
+    (as a serving front end's pooled response buffers are); carved from
+    `arena` when given."""
     import torch
 
     import lbvh_gb300 as lb
 
-    outs = [np.empty(d.shape[0], lb.HIT_DTYPE) if k == "trace" else None for _, k, _, d in reqs]
+    def hits(m):
+        if arena is None:
+            return np.empty(m, lb.HIT_DTYPE)
+        return arena.take(16 * m).view(lb.HIT_DTYPE)
+
+    outs = [hits(d.shape[0]) if k == "trace" else None for _, k, _, d in reqs]
     zeros = torch.zeros((max([o.shape[0] for o in outs if o is not None] + [1]), 4), device=device)
     for o in outs:
         if o is not None and o.shape[0]:
@@ -275,15 +334,20 @@ def _result_buffers(reqs, device):
     return outs
 
 
-def _served_run(reqs, device, slots=SERVE_SLOTS):
+def _served_run(reqs, device, slots=SERVE_SLOTS, buffers="pageable"):
     """One arrival stream through the request server and through the plain
     API; latency from each request's (nominal) arrival. Both paths write
-    trace hits into caller-provided, already mapped result buffers."""
+    trace hits into caller-provided, already mapped result buffers; with
+    buffers="pinned" the request arrays and the hit buffers of both paths
+    are page-locked host memory (one arena), else pageable arrays."""
     import torch
 
     from lbvh_gb300 import scenes
     from lbvh_gb300.serve import Server, run_plain
 
+    arena = None
+    if buffers == "pinned":
+        arena, reqs = _pinned_requests(reqs)
     # every request array is copied to the device once before either path
     # runs, so neither pays the first device access to its pages
     seen = set()
@@ -291,8 +355,8 @@ def _served_run(reqs, device, slots=SERVE_SLOTS):
         if id(data) not in seen:
             seen.add(id(data))
             torch.from_numpy(np.ascontiguousarray(data)).to(device)
-    outs_srv = _result_buffers(reqs, device)
-    outs_plain = _result_buffers(reqs, device)
+    outs_srv = _result_buffers(reqs, device, arena)
+    outs_plain = _result_buffers(reqs, device, arena)
     torch.cuda.synchronize()
     with Server(device, slots=slots, hbm_budget=120 << 30) as srv:
         srv.submit("build", -1, scenes.soup(1000, 1)).result()  # library warm-up
@@ -328,6 +392,7 @@ def _served_run(reqs, device, slots=SERVE_SLOTS):
     kinds = [k for _, k, _, _ in reqs]
     out = {"requests": len(reqs), "mix": {k: kinds.count(k) for k in ("build", "refit", "trace")},
            "worker_streams": slots, "results": "caller-provided hit buffers, mapped before the run (both paths)",
+           "host_buffers": buffers,
            "server": {"p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99), "throughput_req_s": round(len(lat) / span, 1),
                       "trace_mrays_s": round(rays / span / 1e6, 1), "coalesced_requests": coalesced,
                       "evictions": evictions,
@@ -341,24 +406,31 @@ def _served_run(reqs, device, slots=SERVE_SLOTS):
     return out
 
 
-def measure_served(device, seed=7):
+def measure_served(device, seed=7, buffers="pinned"):
     """Served workloads (Poisson arrivals of build / refit / trace requests on
     48 resident scenes, 70% trace / 20% refit / 10% rebuild after one build
-    per scene) through the request server (4 streams, coalescing, 120 GB HBM
-    budget), against the same arrivals through the plain API one request at a
+    per scene) through the request server (16 worker streams, coalescing,
+    120 GB HBM budget), against the same arrivals through the plain API one request at a
     time:
       mix:   scenes 1k-2M triangles, traces 16k-2M rays, 400 requests at
              2,000 requests/s;
       small: scenes 1k-64k triangles, traces 16k-64k rays, 2,000 requests at
-             200,000 requests/s (a burst: both paths saturated)."""
+             200,000 requests/s (a burst: both paths saturated).
+    `buffers` picks the host memory of the request arrays and hit buffers
+    (the same for both paths): one "pinned" arena (the default, as a serving
+    front end's pooled I/O buffers are) or "pageable" arrays."""
     from lbvh_gb300 import scenes
 
     mix = scenes.served_requests(400, 2000.0, seed, n_scenes=48)
-    out = {"mix": dict(rate_per_s=2000.0, scenes=48, **_served_run(mix, device))}
+    out = {"mix": dict(rate_per_s=2000.0, scenes=48, **_served_run(mix, device, buffers=buffers))}
     del mix
     small = scenes.served_requests(2000, 200000.0, seed + 1, n_scenes=48, lo=1000, hi=65536, ray_lo=16384,
                                    ray_hi=65536)
-    out["small"] = dict(rate_per_s=200000.0, scenes=48, **_served_run(small, device))
+    out["small"] = dict(rate_per_s=200000.0, scenes=48, **_served_run(small, device, buffers=buffers))
+    import torch
+
+    if hasattr(torch._C, "_host_emptyCache"):
+        torch._C._host_emptyCache()  # hand the pinned arenas' pages back
     return out
 
 
@@ -512,6 +584,8 @@ def main():
     ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the served-requests measurement")
     ap.add_argument("--only-served", action="store_true", help="only the served-requests measurement")
+    ap.add_argument("--served-buffers", default="pinned", choices=["pinned", "pageable"],
+                    help="host memory of the served requests' arrays and hit buffers (both paths)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -536,7 +610,7 @@ def main():
     ctx = lb.Context(local, stream.cuda_stream)
 
     if args.only_served:
-        r = measure_served(local)
+        r = measure_served(local, buffers=args.served_buffers)
         if rank == 0:
             print(json.dumps({"served": r}), flush=True)
         return 0
@@ -646,7 +720,7 @@ def main():
     # ---- served requests vs the plain path (before the large workloads) ---
     served = None
     if not args.no_served:
-        served = measure_served(local)
+        served = measure_served(local, buffers=args.served_buffers)
 
     # ---- 16M-triangle build (roofline workload) ----------------------------
     build_16m = None

@@ -22,23 +22,41 @@ import math
 
 import numpy as np
 
-_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 
-def _splitmix(x: np.ndarray) -> np.ndarray:
-    x = x + np.uint64(0x9E3779B97F4A7C15)
-    x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-    x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-    return x ^ (x >> np.uint64(31))
+_C1, _C2, _C3 = np.uint64(0x9E3779B97F4A7C15), np.uint64(0xBF58476D1CE4E5B9), np.uint64(0x94D049BB133111EB)
+_CHUNK = 1 << 16  # elements per block of the hash (a few L2-resident temporaries)
+
+
+def _splitmix(x: np.ndarray, t: np.ndarray) -> None:
+    """The splitmix64 finaliser applied to x in place (t: scratch)."""
+    np.add(x, _C1, out=x)
+    for shift, mul in ((30, _C2), (27, _C3)):
+        np.right_shift(x, np.uint64(shift), out=t)
+        np.bitwise_xor(x, t, out=x)
+        np.multiply(x, mul, out=x)
+    np.right_shift(x, np.uint64(31), out=t)
+    np.bitwise_xor(x, t, out=x)
 
 
 def uniform(seed: int, stream: int, n: int, start: int = 0) -> np.ndarray:
-    """n float64 uniforms in [0, 1) (53-bit), element i keyed by start + i."""
+    """n float64 uniforms in [0, 1) (53-bit), element i keyed by start + i:
+    splitmix64(splitmix64(i ^ key) + key) >> 11, scaled by 2^-53."""
+    out = np.empty(n, np.float64)
     with np.errstate(over="ignore"):
         key = np.uint64((seed * 0x632BE59BD9B4E019 + stream * 0x85EBCA77C2B2AE63) & 0xFFFFFFFFFFFFFFFF)
-        idx = np.arange(start, start + n, dtype=np.uint64)
-        h = _splitmix(_splitmix(idx ^ key) + key)
-    return (h >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+        x, t = np.empty(_CHUNK, np.uint64), np.empty(_CHUNK, np.uint64)
+        for a in range(0, n, _CHUNK):
+            m = min(_CHUNK, n - a)
+            xa, ta = x[:m], t[:m]
+            xa[:] = np.arange(start + a, start + a + m, dtype=np.uint64)
+            np.bitwise_xor(xa, key, out=xa)
+            _splitmix(xa, ta)
+            np.add(xa, key, out=xa)
+            _splitmix(xa, ta)
+            np.right_shift(xa, np.uint64(11), out=xa)
+            np.multiply(xa, 1.0 / 9007199254740992.0, out=out[a : a + m], casting="unsafe")
+    return out
 
 
 def normal(seed: int, stream: int, n: int, start: int = 0) -> np.ndarray:
