@@ -173,10 +173,13 @@ release(DevBuf& b, cudaStream_t s)
   b.cap = 0;
 }
 
+// One primitive per thread up to 4 CTAs per SM: a thread's primitives are
+// loaded one after another, so at small sizes every extra primitive per
+// thread adds a memory round trip to the kernel.
 uint32_t
 bounds_blocks_for(const lbvh_ctx* c, uint32_t n)
 {
-  const uint32_t want = ceil_div_u32(n, kBoundsThreads * 8);
+  const uint32_t want = ceil_div_u32(n, kBoundsThreads);
   const uint32_t cap = uint32_t(c->num_sms) * 4;
   return want < 1 ? 1 : (want > cap ? cap : want);
 }
