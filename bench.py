@@ -56,6 +56,19 @@ def measured_traffic(key: str, field: str):
         return None
 
 
+def measured_profile(key: str, fields):
+    """Figures of one kernel's committed ncu capture (profiles/traffic.json),
+    with the summary they come from; None when absent."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)[key]
+        out = {k: d[k] for k in fields if k in d}
+        return dict(out, source="profiles/" + d["summary"]) if out else None
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -715,7 +728,9 @@ def main():
                 "frac": round(trace_bytes / (trace_mean * 1e-3) / 1e9 / hbm_peak, 5),
                 "traffic": measured_traffic("k_trace_tris", "dram_bytes_per_launch"),
                 "algorithmic_bytes": trace_bytes, "peak_kind": peak_kind,
-                "note": "traversal is latency/issue bound; see build_16m for the HBM-bound build"}
+                "note": "traversal is latency/issue bound; see build_16m for the HBM-bound build",
+                "ncu": measured_profile("k_trace_tris", ("l1_hit_rate", "l2_hit_rate", "issue_slots_busy",
+                                                         "warps_active_of_max", "simt_threads_per_instruction"))}
 
     # ---- served requests vs the plain path (before the large workloads) ---
     served = None
