@@ -98,6 +98,32 @@ def test_port_matches_reference_boxes():
     assert nodes_equal(oracle.port().build_boxes(boxes, 4), REF.build_boxes(boxes, 4))
 
 
+@pytest.mark.skipif(REF is None, reason="reference not built on this machine")
+def test_port_matches_reference_extreme_inputs(port):
+    """The inputs of the GPU suite's edge-case traversal and signed-zero
+    tests, through the port and the reference: far-out triangles (boxes
+    beyond 2^60), nearly axis-parallel rays, -0.0 direction components, far
+    origins, and vertex coordinates that are +0.0 and -0.0 in turn."""
+    t = scenes.soup(3000, seed=12)
+    far = scenes.soup(8, seed=13) * np.float32(1e30)
+    t = np.concatenate([t, far]).astype(np.float32)
+    nodes = REF.build(t, 4)
+    assert nodes_equal(port.build(t, 4), nodes)
+    rays = scenes.incoherent_rays(t[:3000], 20_000, 14)
+    rays[::7, 3] = np.float32(1e-30)
+    rays[1::11, 4] = np.float32(-0.0)
+    rays[2::13, 0:3] *= np.float32(1e25)
+    assert hit_mismatches(port.trace(nodes, t, rays, 4), REF.trace(nodes, t, rays, 4)).size == 0
+    rng = np.random.default_rng(15)
+    v = rng.uniform(-1, 1, (4000, 9)).astype(np.float32)
+    zero = rng.random(v.shape) < 0.3
+    v[zero] = np.where(rng.random(zero.sum()) < 0.5, np.float32(0.0), np.float32(-0.0))
+    tz = scenes.make_triangles(v)
+    assert nodes_equal(port.build(tz, 4), REF.build(tz, 4))
+    for a, b in zip(port.curve(tz, 4), REF.curve(tz, 4)):
+        assert np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("name", SPHERE_GOLDEN)
 def test_port_matches_golden_spheres(port, name):
     """User primitives: the example program's spheres, boxes from its
