@@ -360,7 +360,10 @@ def _served_run(reqs, device, slots=SERVE_SLOTS, buffers="pageable"):
 
     arena = None
     if buffers == "pinned":
-        arena, reqs = _pinned_requests(reqs)
+        try:
+            arena, reqs = _pinned_requests(reqs)
+        except RuntimeError as e:  # the host would not lock that much memory
+            buffers = "pageable (page-locking failed: " + str(e).splitlines()[0][:120] + ")"
     # every request array is copied to the device once before either path
     # runs, so neither pays the first device access to its pages
     seen = set()
