@@ -53,3 +53,16 @@ int main(void) {
         r = subprocess.run([cc, "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), path, "-o", exe,
                             lib_built], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """With the CUDA library absent the package raises instead of computing
+    anything on the CPU."""
+    import lbvh_gb300 as lb
+
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "liblbvh_gb300.so"))
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        _lib.lib()
+    with pytest.raises(ImportError):
+        lb.Context(0, 0)
