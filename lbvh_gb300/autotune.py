@@ -34,9 +34,10 @@ def load_table(path: str | None = None) -> dict:
     path = path or cache_path()
     try:
         with open(path) as f:
-            return json.load(f)
+            table = json.load(f)
     except (OSError, ValueError):
         return {}
+    return table if isinstance(table, dict) else {}  # not a table: start a new one
 
 
 def save_table(table: dict, path: str | None = None) -> None:
