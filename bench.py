@@ -9,8 +9,13 @@ rays per step. `value` is rays per second over whole steps (build included),
 in Mrays/s; `build` and `trace` give the two stages alone. The L2 (129 MB) is
 flushed by writing a 256 MB buffer between timed steps, outside the timing.
 
-Also measured (not part of the step): the build of a 16M-triangle random soup,
-the workload of the HBM roofline (`build_16m`), timed per stage.
+Also measured (not part of the step): `e2e`, the same step through the public
+API from page-locked host buffers; the build of a 16M-triangle random soup,
+the workload of the HBM roofline (`build_16m`, with a refit); 4,096 meshes
+built and traced as one batch against the plain per-mesh path (`batched`);
+and Poisson request streams through the request server against the plain
+path (`served`; request arrays and hit buffers page-locked for both paths
+unless --served-buffers pageable).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
