@@ -99,6 +99,21 @@ def test_port_matches_reference_boxes():
 
 
 @pytest.mark.skipif(REF is None, reason="reference not built on this machine")
+def test_port_matches_reference_at_gpu_test_sizes(port):
+    """The port against the reference at the sizes the GPU suite compares
+    the library with the port: a 300,007-triangle soup, the 262,267-triangle
+    room scene, and the 1.6M-triangle soup with 18,000 equal triangles."""
+    for t, m in ((scenes.soup(300_007, 300_007), 1024), (scenes.room_scene(seed=2), 4096)):
+        nodes = REF.build(t, 8)
+        assert nodes_equal(port.build(t, 8), nodes)
+        rays = scenes.incoherent_rays(t, m, 7)
+        assert hit_mismatches(port.trace(nodes, t, rays, 8), REF.trace(nodes, t, rays, 8)).size == 0
+    t = scenes.soup_large(1_600_000, seed=90)
+    t[:18_000] = t[0]
+    assert nodes_equal(port.build(t, 16), REF.build(t, 16))
+
+
+@pytest.mark.skipif(REF is None, reason="reference not built on this machine")
 def test_port_matches_reference_extreme_inputs(port):
     """The inputs of the GPU suite's edge-case traversal and signed-zero
     tests, through the port and the reference: far-out triangles (boxes
