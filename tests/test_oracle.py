@@ -114,6 +114,14 @@ def test_port_matches_reference_at_gpu_test_sizes(port):
 
 
 @pytest.mark.skipif(REF is None, reason="reference not built on this machine")
+def test_port_matches_reference_16m_soup(port):
+    """The roofline workload, the 16M-triangle soup, built by the port and
+    by the reference (about 15 s with the generation)."""
+    t = scenes.soup_large(16_000_000, seed=16)
+    assert nodes_equal(port.build(t, 16), REF.build(t, 16))
+
+
+@pytest.mark.skipif(REF is None, reason="reference not built on this machine")
 def test_port_matches_reference_extreme_inputs(port):
     """The inputs of the GPU suite's edge-case traversal and signed-zero
     tests, through the port and the reference: far-out triangles (boxes
