@@ -1,23 +1,31 @@
 """LBVH build + closest-hit trace benchmark on one GB300 (or N replicas).
 
-Default workload (one "step"): the mid-size coherent scene -- a 6,320-triangle
-torus plus a 2,000-triangle ground plane (8,320 triangles) -- is built from
-device-resident triangles and traced with 1024 x 1024 primary rays from a
-pinhole camera at (0, 0, 3) (60 deg) plus 1,048,576 incoherent rays (origins
-uniform in 1.5x the scene box, directions uniform on the sphere): 2,097,152
-rays per step. `value` is rays per second over whole steps (build included),
-in Mrays/s; `build` and `trace` give the two stages alone. The L2 (129 MB) is
-flushed by writing a 256 MB buffer between timed steps, outside the timing.
+Default workload (one "step"), the large clustered scene: a room of 262,267
+triangles (walls, 64 columns, 500 clutter clusters; generation order kept,
+so leaf p is primitive p as in the reference) is built from device-resident
+triangles, then traced with 1920 x 1080 primary rays from a pinhole camera
+and with one cosine-weighted diffuse bounce ray per primary hit. The bounce
+rays are made once, before timing, from the primary hits (bit-identical on
+both arms), so every step traces the same 4.1M rays. `value` is rays per
+second over whole steps (build included), in Mrays/s; `build` and `trace`
+give the stages alone. The L2 (129 MB) is flushed by writing a 256 MB buffer
+between timed steps, outside the timing.
 
-Also measured (not part of the step): `e2e`, the same step through the public
-API from page-locked host buffers; the build of a 16M-triangle random soup,
-the workload of the HBM roofline (`build_16m`, with a refit); 4,096 meshes
+Also measured (not part of the step): `e2e`, the same step through the
+public API from page-locked host buffers; the build of a 16M-triangle random
+soup, the workload of the HBM roofline (`build_16m`, with a refit; the
+headline `roofline`); the mid-size torus step (`config1`); 4,096 meshes
 built and traced as one batch against the plain per-mesh path (`batched`);
 and Poisson request streams through the request server against the plain
-path (`served`; request arrays and hit buffers page-locked for both paths
-unless --served-buffers pageable).
+path (`served`). Full records of those sections are printed as `detail`
+lines before the final line, which carries their summaries.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the unmodified reference (lbvh::builder<float> and
+lbvh::traverser, compiled from the staged reference files into
+oracle/_ref/libref.so; the bit-exact restatement only where they are absent)
+on the same step, the same rays, all host cores.
 
 Under torchrun (N > 1) every rank runs an independent replica of the same
 step on its own GPU ("replicas only": the path has no exchange step); value
@@ -40,7 +48,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Build Mprims/s + trace Mrays/s (1 GB300)"
-WORKLOAD = "torus8320_primary1024x1024_incoherent1M"
+WORKLOAD = "room262267_primary1920x1080_diffusebounce"
+CONFIG1_WORKLOAD = "torus8320_primary1024x1024_incoherent1M"
+L2_POLICY = "GPU arm: L2 flushed (256 MB write) between timed steps"
+LEAF_ORDER = "reference parity (leaf p = primitive p)"
 N_BUILD_16M = 16_000_000
 # Algorithmic HBM bytes per primitive of an LBVH build, by stage: the fixed
 # yardstick of the roofline (read the 36 used bytes of a triangle for the
@@ -169,41 +180,81 @@ def dist_setup():
 # reference arm: the reference's CPU implementation on the host cores
 
 
+def room_workload():
+    """The large clustered scene and its primary rays: 262,267 triangles,
+    1920 x 1080 pinhole rays from inside the room."""
+    from lbvh_gb300 import scenes
+
+    tris = scenes.room_scene(seed=21)
+    prim = scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))
+    return tris, prim
+
+
+def room_bounce(prim, hits, tris):
+    """One cosine-weighted diffuse bounce ray per primary hit."""
+    from lbvh_gb300 import scenes
+
+    return scenes.diffuse_bounce(prim, hits, tris, seed=22)
+
+
+def room_config(tris, prim, bounce, world):
+    """The step's config, identical on both arms (the digest covers every
+    ray the step traces)."""
+    import hashlib
+
+    h = hashlib.sha1(prim.tobytes())
+    h.update(bounce.tobytes())
+    return {"workload": WORKLOAD, "triangles": int(tris.shape[0]), "primary_rays": int(prim.shape[0]),
+            "bounce_rays": int(bounce.shape[0]), "rays_per_step": int(prim.shape[0] + bounce.shape[0]),
+            "rays_sha1": h.hexdigest()[:16], "parallelism": f"replicas{world}", "l2": L2_POLICY,
+            "leaf_order": LEAF_ORDER}
+
+
+def cpu_impl():
+    """The reference's own CPU builder and traverser (oracle/_ref/libref.so,
+    compiled from the unmodified reference header), else the bit-exact port."""
+    import oracle
+
+    impl = oracle.ref()
+    if impl is not None:
+        return impl, "reference", impl.path
+    impl = oracle.port()
+    return impl, "port", impl.path
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
-    import oracle
-    from lbvh_gb300 import scenes
-
-    impl = oracle.ref()
-    kind = "reference"
-    if impl is None:
-        impl, kind = oracle.port(), "port"
+    impl, kind, path = cpu_impl()
     cores = os.cpu_count() or 1
-    tris = scenes.torus_scene(seed=11)
-    rays = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(tris, 1 << 20, 3)])
-    # bounded sample: every 8th ray (262,144 rays) per step
-    sample = np.ascontiguousarray(rays[::8])
+    tris, prim = room_workload()
+    nodes = impl.build(tris, cores)
+    bounce = room_bounce(prim, impl.trace(nodes, tris, prim, cores), tris)
+    m = prim.shape[0] + bounce.shape[0]
+    # warm-up steps: the whole build, rays sampled (nothing on the CPU warms
+    # up beyond first-touch of the buffers)
     for _ in range(args.warmup):
         nodes = impl.build(tris, cores)
-        impl.trace(nodes, tris, sample[:4096], cores)
+        impl.trace(nodes, tris, prim[::64], cores)
+        impl.trace(nodes, tris, bounce[::64], cores)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         nodes = impl.build(tris, cores)
-        impl.trace(nodes, tris, sample, cores)
+        impl.trace(nodes, tris, prim, cores)
+        impl.trace(nodes, tris, bounce, cores)
         times.append(time.perf_counter() - t0)
     ms = 1e3 * float(np.mean(times))
-    value = sample.shape[0] / (ms * 1e-3) / 1e6
+    value = m / (ms * 1e-3) / 1e6
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s",
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mrays/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "triangles": int(tris.shape[0]), "rays_per_step": int(sample.shape[0]),
-                   "sample": "every 8th ray of the 2,097,152-ray step", "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": cores, "kind": kind,
-                         "sample": f"build of all {tris.shape[0]} triangles + {sample.shape[0]} rays per step"},
-        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": room_config(tris, prim, bounce, world),
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": kind,
+                         "lib": os.path.relpath(path, ROOT),
+                         "sample": f"the whole step: build of all {tris.shape[0]} triangles + all {m} rays"},
+        "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -590,6 +641,76 @@ def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_
 # our arm
 
 
+def time_steps(builder, bvh, trav, tris, ray_sets, hit_sets, flush, stream, steps):
+    """K whole steps (build, then one trace per ray set) timed with CUDA
+    events on the launching stream, L2 flushed before each step. Returns
+    per-step (build ms, trace ms)."""
+    import torch
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2 + len(ray_sets))] for _ in range(steps)]
+    torch.cuda.synchronize()
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        builder(tris, into=bvh)
+        ev[i][1].record(stream)
+        for k, (r, h) in enumerate(zip(ray_sets, hit_sets)):
+            trav(r, out=h)
+            ev[i][2 + k].record(stream)
+    torch.cuda.synchronize()
+    return [(e[0].elapsed_time(e[1]), e[1].elapsed_time(e[-1])) for e in ev]
+
+
+def measure_config1(ctx, stream, flush, dev, steps):
+    """The mid-size coherent scene (8,320 triangles: torus + ground plane),
+    1024 x 1024 primary + 1,048,576 incoherent rays, build included."""
+    import torch
+
+    import lbvh_gb300 as lb
+    from lbvh_gb300 import scenes
+
+    tris_h = scenes.torus_scene(seed=11)
+    rays_h = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(tris_h, 1 << 20, 3)])
+    tris = torch.from_numpy(tris_h).to(dev)
+    rays = torch.from_numpy(rays_h).to(dev)
+    hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+    builder, bvh = lb.Builder(ctx), lb.BVH(ctx)
+    builder(tris, into=bvh)
+    trav = lb.Traverser(bvh)
+    for _ in range(3):
+        builder(tris, into=bvh)
+        trav(rays, out=hits)
+    t = time_steps(builder, bvh, trav, tris, [rays], [hits], flush, stream, steps)
+    b, tr = float(np.mean([x for x, _ in t])), float(np.mean([y for _, y in t]))
+    m = rays.shape[0]
+    return {"workload": CONFIG1_WORKLOAD, "triangles": int(tris_h.shape[0]), "rays_per_step": int(m),
+            "value": round(m / ((b + tr) * 1e-3) / 1e6, 1), "unit": "Mrays/s", "ms_per_step": round(b + tr, 4),
+            "build_ms": round(b, 4), "trace_ms": round(tr, 4)}
+
+
+def summary_line(line):
+    """The final JSON line: the contract's keys plus one-line summaries of
+    the extra sections (their full records are the detail lines above)."""
+    out = {k: v for k, v in line.items() if k not in ("build_16m", "batched", "served", "config1")}
+    b16 = line.get("build_16m")
+    if b16:
+        out["build_16m"] = {"ms": b16["ms"], "mprims_s": b16["mprims_s"], "refit_ms": b16["refit_ms"],
+                            "frac": b16["roofline"]["frac"]}
+    c1 = line.get("config1")
+    if c1:
+        out["config1"] = {k: c1[k] for k in ("value", "ms_per_step", "build_ms", "trace_ms")}
+    bt = line.get("batched")
+    if bt:
+        out["batched"] = {"graph_step_ms": bt.get("graph_step_ms"), "plain_step_ms": bt["plain_step_ms"],
+                          "speedup_vs_plain": bt["speedup_vs_plain"],
+                          "sorted_leaves_step_ms": bt["sorted_leaves"]["step_ms"]}
+    sv = line.get("served")
+    if sv:
+        out["served"] = {k: {"ratio": v["throughput_ratio"], "p99_ms": [v["server"]["p99_ms"], v["plain"]["p99_ms"]],
+                             "equal": v["results_equal"]} for k, v in sv.items()}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -601,6 +722,10 @@ def main():
     ap.add_argument("--soup-n", type=int, default=N_BUILD_16M, help="soup size of the build measurement")
     ap.add_argument("--soup-span", type=float, default=1.0,
                     help="profiling: stretch the soup's bounds to +-span (denser Morton buckets)")
+    ap.add_argument("--only-step", action="store_true", help="only the headline step (profiling)")
+    ap.add_argument("--step-rays", type=int, default=0,
+                    help="profiling: trace only every k-th ray of the headline step (0: all)")
+    ap.add_argument("--no-config1", action="store_true", help="skip the mid-size torus step")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
     ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the served-requests measurement")
@@ -622,7 +747,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     import lbvh_gb300 as lb
-    from lbvh_gb300 import _build, scenes
+    from lbvh_gb300 import _build
 
     _build.build()
     hbm_peak, peak_kind = peaks()
@@ -630,52 +755,50 @@ def main():
     stream = torch.cuda.current_stream(dev)
     ctx = lb.Context(local, stream.cuda_stream)
 
+    def detail(name, rec):
+        if rank == 0:
+            print(json.dumps({"detail": name, name: rec}), flush=True)
+
     if args.only_served:
-        r = measure_served(local, buffers=args.served_buffers)
-        if rank == 0:
-            print(json.dumps({"served": r}), flush=True)
+        detail("served", measure_served(local, buffers=args.served_buffers))
         return 0
-
     if args.only_batched:
-        r = measure_batched(local, args.steps, hbm_peak, peak_kind)
-        if rank == 0:
-            print(json.dumps({"batched": r}), flush=True)
+        detail("batched", measure_batched(local, args.steps, hbm_peak, peak_kind))
         return 0
-
-    if args.only_16m:
-        flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
-        r = measure_build_16m(ctx, lb.Builder(ctx), stream, flush, dev, args.steps, hbm_peak, peak_kind,
-                              args.soup_n, args.soup_span)
-        if rank == 0:
-            print(json.dumps({"build_16m": r}), flush=True)
-        return 0
-
-    tris_h = scenes.torus_scene(seed=11)
-    rays_h = np.concatenate([scenes.pinhole_rays(1024, 1024), scenes.incoherent_rays(tris_h, 1 << 20, 3)])
-    n, m = tris_h.shape[0], rays_h.shape[0]
-    tris = torch.from_numpy(tris_h).to(dev)
-    rays = torch.from_numpy(rays_h).to(dev)
-    hits = torch.empty((m, 4), dtype=torch.float32, device=dev)
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MB > L2
+    if args.only_16m:
+        detail("build_16m", measure_build_16m(ctx, lb.Builder(ctx), stream, flush, dev, args.steps, hbm_peak,
+                                              peak_kind, args.soup_n, args.soup_span))
+        return 0
+
+    # ---- the step's inputs: the room, its primary rays, the bounce rays ---
+    tris_h, prim_h = room_workload()
+    if args.step_rays > 1:
+        prim_h = np.ascontiguousarray(prim_h[:: args.step_rays])
+    n = tris_h.shape[0]
+    tris = torch.from_numpy(tris_h).to(dev)
+    prim = torch.from_numpy(prim_h).to(dev)
+    hits_p = torch.empty((prim.shape[0], 4), dtype=torch.float32, device=dev)
     builder = lb.Builder(ctx)
     bvh = lb.BVH(ctx)
-    ctx.reserve(n, m)
-    trav = None
-
-    def step():
-        nonlocal trav
-        builder(tris, into=bvh)
-        if trav is None:
-            trav = lb.Traverser(bvh)
-        trav(rays, out=hits)
+    ctx.reserve(n, prim.shape[0])
+    builder(tris, into=bvh)
+    trav = lb.Traverser(bvh)
+    trav(prim, out=hits_p)
+    torch.cuda.synchronize()
+    bounce_h = room_bounce(prim_h, lb.hits_view(hits_p), tris_h)  # made once, before timing
+    bounce = torch.from_numpy(bounce_h).to(dev)
+    hits_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32, device=dev)
+    m = prim.shape[0] + bounce.shape[0]
+    config = room_config(tris_h, prim_h, bounce_h, world)
 
     for _ in range(args.warmup):
-        step()
+        builder(tris, into=bvh)
+        trav(prim, out=hits_p)
+        trav(bounce, out=hits_b)
     torch.cuda.synchronize()
 
     # ---- timed region: K whole steps --------------------------------------
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -683,129 +806,133 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     clocks.mark(True)
-    for i in range(args.steps):
-        flush.zero_()
-        ev[i][0].record(stream)
-        builder(tris, into=bvh)
-        ev[i][1].record(stream)
-        trav(rays, out=hits)
-        ev[i][2].record(stream)
-    torch.cuda.synchronize()
+    t = time_steps(builder, bvh, trav, tris, [prim, bounce], [hits_p, hits_b], flush, stream, args.steps)
     clocks.mark(False)
     if world > 1:
         dist.barrier()
     clk = clocks.stop()
-    build_ms = [a.elapsed_time(b) for a, b, _ in ev]
-    trace_ms = [b.elapsed_time(c) for _, b, c in ev]
-    step_ms = float(np.mean([x + y for x, y in zip(build_ms, trace_ms)]))
-    step_ms, value = replica_throughput(step_ms, m, world, dev)
-    gpu_launches = args.steps * (8 + 2)  # bounds, Morton, 4 sort passes, local + global tree; repack, trace
+    build_ms = float(np.mean([x for x, _ in t]))
+    trace_ms = float(np.mean([y for _, y in t]))
+    step_ms, value = replica_throughput(build_ms + trace_ms, m, world, dev)
+    # per step: bounds, Morton, four onesweep passes, local + global tree
+    # phases; the traversal copy (k_repack); two traversals
+    gpu_launches = args.steps * (8 + 1 + 2)
 
-    # correctness guard on the timed output: the same hits as an untimed run
-    ref_hits = torch.empty_like(hits)
-    lb.Traverser(lb.Builder(ctx)(tris))(rays, out=ref_hits)
+    # correctness guard on the timed output: the same hits as a fresh build
+    ref_p = torch.empty_like(hits_p)
+    ref_b = torch.empty_like(hits_b)
+    fresh = lb.Traverser(lb.Builder(ctx)(tris))
+    fresh(prim, out=ref_p)
+    fresh(bounce, out=ref_b)
     torch.cuda.synchronize()
-    assert torch.equal(ref_hits.view(torch.int32), hits.view(torch.int32))
-    hv = lb.hits_view(hits)
-    hit_frac = float(np.mean(hv["prim"] != lb.MISS))
+    assert torch.equal(ref_p.view(torch.int32), hits_p.view(torch.int32))
+    assert torch.equal(ref_b.view(torch.int32), hits_b.view(torch.int32))
+    hit_frac = float(np.mean(lb.hits_view(hits_p)["prim"] != lb.MISS))
 
-    # ---- e2e: the public API with pinned host buffers ----------------------
-    tris_p = torch.from_numpy(tris_h).pin_memory()
-    rays_p = torch.from_numpy(rays_h).pin_memory()
-    hits_p = torch.empty((m, 4), dtype=torch.float32).pin_memory()
+    # ---- e2e: the public API with page-locked host buffers ---------------
+    tris_pin = torch.from_numpy(tris_h).pin_memory()
+    prim_pin = torch.from_numpy(prim_h).pin_memory()
+    bounce_pin = torch.from_numpy(bounce_h).pin_memory()
+    out_p = torch.empty((prim.shape[0], 4), dtype=torch.float32).pin_memory()
+    out_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32).pin_memory()
     b_e2e = lb.BVH(ctx)
     for _ in range(2):
-        lb.Traverser(builder(tris_p, into=b_e2e))(rays_p, out=hits_p)
+        tr = lb.Traverser(builder(tris_pin, into=b_e2e))
+        tr(prim_pin, out=out_p)
+        tr(bounce_pin, out=out_b)
     e2e_t = []
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        builder(tris_p, into=b_e2e)          # H2D copy of the triangles inside
-        lb.Traverser(b_e2e)(rays_p, out=hits_p)  # rays read / hits written in host memory, sync
+        builder(tris_pin, into=b_e2e)        # H2D copy of the triangles inside
+        tr = lb.Traverser(b_e2e)
+        tr(prim_pin, out=out_p)              # rays read / hits written in host memory, synchronous
+        tr(bounce_pin, out=out_b)
         e2e_t.append(time.perf_counter() - t0)
     e2e_ms = 1e3 * float(np.mean(e2e_t))
-    assert torch.equal(hits_p.view(torch.int32), hits.cpu().view(torch.int32))
-
-    # ---- the trace kernel alone: HBM-normalised view ----------------------
-    trace_mean = float(np.mean(trace_ms))
-    trace_bytes = m * (32 + 16)  # rays in, hits out (the scene stays in L2)
-    roofline = {"bound": "hbm", "kernel": "k_trace_tris",
-                "achieved": round(trace_bytes / (trace_mean * 1e-3) / 1e9, 2),
-                "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(trace_bytes / (trace_mean * 1e-3) / 1e9 / hbm_peak, 5),
-                "traffic": measured_traffic("k_trace_tris", "dram_bytes_per_launch"),
-                "algorithmic_bytes": trace_bytes, "peak_kind": peak_kind,
-                "note": "traversal is latency/issue bound; see build_16m for the HBM-bound build",
-                "ncu": measured_profile("k_trace_tris", ("l1_hit_rate", "l2_hit_rate", "issue_slots_busy",
-                                                         "warps_active_of_max", "simt_threads_per_instruction"))}
-
-    # ---- served requests vs the plain path (before the large workloads) ---
-    served = None
-    if not args.no_served:
-        served = measure_served(local, buffers=args.served_buffers)
-
-    # ---- 16M-triangle build (roofline workload) ----------------------------
-    build_16m = None
-    if not args.no_16m:
-        del tris_p, rays_p, hits_p
-        build_16m = measure_build_16m(ctx, builder, stream, flush, dev, args.steps, hbm_peak, peak_kind,
-                                      args.soup_n, with_refit=True)
-
-    # ---- batched meshes (4,096 soups) vs the plain per-mesh path ----------
-    batched = None
-    if not args.no_batched:
-        batched = measure_batched(local, args.steps, hbm_peak, peak_kind)
-
-    # ---- CPU baseline: the oracle port (or reference) on the host cores ---
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        import oracle
-        impl = oracle.ref()
-        kind = "reference"
-        if impl is None:
-            impl, kind = oracle.port(), "port"
-        cores = os.cpu_count() or 1
-        sample = np.ascontiguousarray(rays_h[::8])
-        impl.build(tris_h, cores)
-        ts = []
-        for _ in range(3):
-            t0 = time.perf_counter()
-            nodes = impl.build(tris_h, cores)
-            impl.trace(nodes, tris_h, sample, cores)
-            ts.append(time.perf_counter() - t0)
-        cval = sample.shape[0] / float(np.mean(ts)) / 1e6
-        cpu = {"value": round(cval, 3), "unit": "Mrays/s", "cores": cores, "kind": kind,
-               "sample": f"build of all {n} triangles + every 8th ray ({sample.shape[0]}) per step, 3 steps"}
+    assert torch.equal(out_p.view(torch.int32), hits_p.cpu().view(torch.int32))
+    assert torch.equal(out_b.view(torch.int32), hits_b.cpu().view(torch.int32))
+    del tris_pin, prim_pin, bounce_pin, out_p, out_b
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD, "triangles": n, "rays_per_step": m,
-                   "parallelism": f"replicas{world}", "l2": "flushed (256 MB write) between timed steps",
-                   "leaf_order": "reference parity (leaf p = primitive p)"},
-        "build": {"ms": round(float(np.mean(build_ms)), 4),
-                  "mprims_s": round(n / (float(np.mean(build_ms)) * 1e-3) / 1e6, 2)},
-        "trace": {"ms": round(trace_mean, 4), "mrays_s": round(m / (trace_mean * 1e-3) / 1e6, 1),
-                  "hit_fraction": round(hit_frac, 4)},
-        "build_16m": build_16m,
-        "batched": batched,
-        "served": served,
-        "roofline": roofline,
-        "cpu_baseline": cpu,
-        "e2e": {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
-                "ms_per_step": round(e2e_ms, 4),
-                "h2d_bytes_per_step": int(tris_h.nbytes + rays_h.nbytes),
-                "d2h_bytes_per_step": int(m * 16),
-                "transfer": "triangles copied; rays read and hits written in place in page-locked host "
-                            "memory over NVLink-C2C (hits in 512-byte warp batches)"},
-        "gpu_launches": gpu_launches,
-        "clocks": clk,
+        "data": "synthetic", "config": config,
+        "build": {"ms": round(build_ms, 4), "mprims_s": round(n / (build_ms * 1e-3) / 1e6, 1)},
+        "trace": {"ms": round(trace_ms, 4), "mrays_s": round(m / (trace_ms * 1e-3) / 1e6, 1),
+                  "primary_hit_fraction": round(hit_frac, 4)},
     }
+    if args.only_step:
+        line["gpu_launches"] = gpu_launches
+        line["clocks"] = clk
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
+
+    # ---- the mid-size torus step -------------------------------------------
+    if not args.no_config1:
+        line["config1"] = measure_config1(ctx, stream, flush, dev, args.steps)
+        detail("config1", line["config1"])
+
+    # ---- served requests vs the plain path (before the large workloads) ---
+    if not args.no_served:
+        line["served"] = measure_served(local, buffers=args.served_buffers)
+        detail("served", line["served"])
+
+    # ---- 16M-triangle build: the HBM roofline workload ---------------------
+    if not args.no_16m:
+        line["build_16m"] = measure_build_16m(ctx, builder, stream, flush, dev, args.steps, hbm_peak, peak_kind,
+                                              args.soup_n, with_refit=True)
+        detail("build_16m", line["build_16m"])
+
+    # ---- batched meshes (4,096 soups) vs the plain per-mesh path ----------
+    if not args.no_batched:
+        line["batched"] = measure_batched(local, args.steps, hbm_peak, peak_kind)
+        detail("batched", line["batched"])
+
+    # ---- roofline: the build (HBM-bound) at 16M triangles, or the step's
+    # own build when that measurement was skipped; the traversal (issue /
+    # latency bound) is described by its ncu figures beside it
+    if line.get("build_16m"):
+        rf = dict(line["build_16m"]["roofline"], kernel="lbvh build, 16M-triangle soup (all build kernels)")
+    else:
+        algo = n * sum(BYTES_PER_PRIM.values())
+        rf = {"bound": "hbm", "kernel": "lbvh build, room scene (all build kernels)",
+              "achieved": round(algo / (build_ms * 1e-3) / 1e9, 1), "peak": hbm_peak, "unit": "GB/s",
+              "frac": round(algo / (build_ms * 1e-3) / 1e9 / hbm_peak, 4),
+              "bytes_per_prim": sum(BYTES_PER_PRIM.values()), "traffic": None, "peak_kind": peak_kind}
+    line["roofline"] = rf
+    line["trace_profile"] = measured_profile("k_trace_room", ("issue_slots_busy", "simt_threads_per_instruction",
+                                                              "l1_hit_rate", "l2_hit_rate", "warps_active_of_max"))
+
+    # ---- CPU baseline: the reference on the host cores (bounded sample) ---
+    if rank == 0 and not args.no_cpu:
+        impl, kind, path = cpu_impl()
+        cores = os.cpu_count() or 1
+        sp, sb = np.ascontiguousarray(prim_h[::16]), np.ascontiguousarray(bounce_h[::16])
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            nodes = impl.build(tris_h, cores)
+            impl.trace(nodes, tris_h, sp, cores)
+            impl.trace(nodes, tris_h, sb, cores)
+            ts.append(time.perf_counter() - t0)
+        cval = (sp.shape[0] + sb.shape[0]) / float(np.mean(ts)) / 1e6
+        line["cpu_baseline"] = {"value": round(cval, 4), "unit": "Mrays/s", "cores": cores, "kind": kind,
+                                "lib": os.path.relpath(path, ROOT),
+                                "sample": f"build of all {n} triangles + every 16th primary and bounce ray "
+                                          f"({sp.shape[0] + sb.shape[0]}) per step, 3 steps"}
+    line["e2e"] = {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+                   "ms_per_step": round(e2e_ms, 4),
+                   "h2d_bytes_per_step": int(tris_h.nbytes + prim_h.nbytes + bounce_h.nbytes),
+                   "d2h_bytes_per_step": int(m * 16),
+                   "transfer": "triangles copied; rays read and hits written in place in page-locked host memory"}
+    line["gpu_launches"] = gpu_launches
+    line["clocks"] = clk
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(summary_line(line)), flush=True)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()

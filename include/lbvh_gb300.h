@@ -128,6 +128,12 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             place, each warp's batch of 32 as one 512-byte store (the
                                             traversal then reaches host memory over the CPU-GPU link);
                                             pageable host memory is always copied */
+#define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
+                                            and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
+                                            seconds); no tree is built after a wait gave up */
+#define LBVH_PARAM_TEST_LOOKBACK_STALL 7 /* test only: 1 makes every look-back wait for a word no tile
+                                            ever writes, so each wait runs out after the spin limit and
+                                            the build reports LBVH_ERR_TIMEOUT; 0 (default) for real use */
 LBVH_API int lbvh_ctx_set_param(lbvh_ctx* ctx, int param, int value);
 
 /* Replaces the reference triangle constructor triangle<float>(a, b, c)
@@ -288,10 +294,13 @@ LBVH_API int lbvh_batch_trace_triangles(lbvh_ctx* ctx, const lbvh_batch* batch, 
  * current device. If d_status is not NULL it receives, in stream order, the
  * build's device error bits (0 = success).
  *
- * The first call on each device looks up the scratch array's device address;
- * make it before capturing any stream. Every call on a device shares the one
- * scratch array: calls whose GPU work overlaps (other streams, other threads)
- * race and corrupt each other, so serialize them per device. */
+ * The first call on each device looks up the scratch array's device address
+ * and keeps it for the life of the process; make it before capturing any
+ * stream, and do not call again on a device after a cudaDeviceReset of it.
+ * Every call clears the scratch it uses before building, so no state
+ * carries over between calls. Every call on a device shares the one scratch
+ * array: calls whose GPU work overlaps (other streams, other threads) race
+ * and corrupt each other, so serialize them per device. */
 LBVH_API int lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint32_t* d_status,
                                           void* stream);
 

@@ -647,6 +647,16 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "trace in-place mode %d outside [0, 2]", value);
       c->trace_in_place = value;
       return LBVH_OK;
+    case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
+      if (value < 1 || value > (1 << 24))
+        return fail(c, LBVH_ERR_INVALID_ARG, "look-back spin limit %d outside [1, 2^24]", value);
+      c->bufs.spin_limit = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_TEST_LOOKBACK_STALL:
+      if (value < 0 || value > 1)
+        return fail(c, LBVH_ERR_INVALID_ARG, "look-back stall %d is not 0 or 1", value);
+      c->bufs.wait_xor = value ? 0x80000000u : 0u; // a tag no tile publishes
+      return LBVH_OK;
     default:
       return fail(c, LBVH_ERR_INVALID_ARG, "unknown parameter %d", param);
   }

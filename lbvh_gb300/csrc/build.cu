@@ -263,7 +263,9 @@ k_onesweep(const uint32_t* __restrict__ kin,
            uint32_t epoch,
            unsigned long long* __restrict__ lookback,
            BuildState* __restrict__ st,
-           bool skip_if_msd)
+           bool skip_if_msd,
+           uint32_t spin_limit,
+           uint32_t wait_xor)
 {
   constexpr int kTile = kSortThreads * kItems;
   if (skip_if_msd && st->use_msd)
@@ -352,6 +354,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
   // and poll again from there.
   uint32_t excl = 0;
   if (tile > 0) {
+    const uint32_t want = epoch ^ wait_xor; // the tag earlier tiles publish (wait_xor: 0)
     uint32_t p = tile - 1; // next tile to read
     uint32_t spins = 0;
     bool done = false;
@@ -367,7 +370,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
           continue;
         const uint32_t lo = uint32_t(e[w]);
         const uint32_t status = lo >> 30;
-        if (uint32_t(e[w] >> 32) != epoch || status == 0)
+        if (uint32_t(e[w] >> 32) != want || status == 0)
           continue; // not yet published: poll again from here
         excl += lo & 0x3fffffffu;
         used++;
@@ -378,7 +381,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
       if (used) {
         p -= used;
         spins = 0;
-      } else if (++spins > kSpinLimit) {
+      } else if (++spins > spin_limit) {
         atomicOr(&st->error, kErrLookbackTimeout);
         break;
       } else if (spins > 64) {
@@ -927,6 +930,10 @@ k_tree_local(Leaf leaf,
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   const uint32_t b0 = blockIdx.x * kTreeBlock;
   const uint32_t count = min(kTreeBlock, n - b0);
+  // A sort that gave up leaves codes in no order, over which a walk could
+  // leave its CTA's ranges: then no tree is built (the error is reported).
+  // The sort kernels have finished, so every thread reads the same bit.
+  const uint32_t sort_failed = __ldcg(&st->error) & kErrLookbackTimeout;
 
   // boundaries k = b0 - 1 .. b0 + kTreeBlock - 1 at s_delta[k - (b0 - 1)]
   for (uint32_t j = tid; j <= kTreeBlock; j += kTreeThreads)
@@ -940,6 +947,8 @@ k_tree_local(Leaf leaf,
     s_npend = 0;
   }
   __syncthreads();
+  if (sort_failed)
+    return;
 
   bool active = false, internal = false;
   uint32_t L = 0, R = 0, lref = 0, rref = 0;
@@ -1067,6 +1076,8 @@ k_tree_global(Leaf leaf,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= min(__ldg(&st->pending_count), uint32_t(gridDim.x * blockDim.x)))
     return;
+  if (__ldcg(&st->error) & kErrLookbackTimeout)
+    return; // the sort gave up: no tree (the error is reported)
   const PendingNode pn = pending_in[i];
   uint32_t L = pn.L, R = pn.R;
   Box box = pn.box;
@@ -1123,6 +1134,8 @@ k_tree_global_cta(Leaf leaf,
                   BuildState* __restrict__ st)
 {
   extern __shared__ uint32_t s_slots[]; // n - 1 split positions
+  if (__ldcg(&st->error) & kErrLookbackTimeout)
+    return; // the sort gave up: no tree (the error is reported); uniform over the CTA
   for (uint32_t j = threadIdx.x; j + 1 < n; j += blockDim.x)
     s_slots[j] = kSlotEmpty;
   __syncthreads();
@@ -1295,7 +1308,8 @@ k_gather_tris(const Tri* __restrict__ tris,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
-  out[i] = tris[__ldg(perm + i)];
+  const uint32_t p = __ldg(perm + i);
+  out[i] = tris[p < n ? p : 0]; // p >= n only after a sort that gave up (error reported)
 }
 
 __global__ void
@@ -1307,7 +1321,8 @@ k_gather_boxes(const Box* __restrict__ boxes,
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
-  out[i] = boxes[__ldg(perm + i)];
+  const uint32_t p = __ldg(perm + i);
+  out[i] = boxes[p < n ? p : 0]; // p >= n only after a sort that gave up (error reported)
 }
 
 // ---------------------------------------------------------------------------
@@ -1370,21 +1385,24 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
   uint32_t* kb = b.keys_b;
   uint32_t* va = b.vals_a;
   uint32_t* vb = b.vals_b;
+  const uint32_t spin = b.spin_limit ? b.spin_limit : kSpinLimit;
+  const uint32_t wx = b.wait_xor;
   for (uint32_t pass = 0; pass < 4; pass++) {
     const uint32_t epoch = epoch_base + pass;
     if (pairs) {
       if (pass == 0)
         k_onesweep<true, true><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, vb, n, pass, epoch, b.lookback, b.state,
-                                                             false);
+                                                             false, spin, wx);
       else
         k_onesweep<true, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, va, vb, n, pass, epoch, b.lookback, b.state,
-                                                              false);
+                                                              false, spin, wx);
     } else if (small) {
       k_onesweep<false, false, kSmallTileItems><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass,
-                                                                              epoch, b.lookback, b.state, msd);
+                                                                              epoch, b.lookback, b.state, msd, spin,
+                                                                              wx);
     } else {
       k_onesweep<false, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass, epoch, b.lookback,
-                                                             b.state, msd);
+                                                             b.state, msd, spin, wx);
     }
     std::swap(ka, kb);
     std::swap(va, vb);

@@ -100,6 +100,9 @@ struct BuildBuffers
   uint32_t msd_group;             // bucket sort: ranges per CTA of the partition
   uint32_t sort_ctas;             // bucket sort: persistent CTAs (one per SM)
   uint32_t* top_rows;             // bucket sort: msd_ranges x kTopBuckets counts (in vals_a)
+  uint32_t spin_limit;            // look-back polls before a wait gives up (0: kSpinLimit)
+  uint32_t wait_xor;              // test only: nonzero makes every look-back wait for a tag no
+                                  // tile publishes, so each wait runs out (0 in normal use)
 };
 
 cudaError_t launch_make_triangles(const float* verts, uint32_t n, Tri* out, cudaStream_t s);

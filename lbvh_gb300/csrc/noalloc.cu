@@ -13,15 +13,20 @@
 // The scratch array is fixed at kNoAllocMaxPrims primitives (about 1.5 MB).
 // Every GPU that loads this library reserves it until the process exits.
 // All calls on a device share it and it keeps the last call's contents, so
-// each call clears the parts that must start at zero (the build counters and
-// the error word). Calls whose work overlaps on the GPU --
-// two streams, or two host threads -- race on the array and corrupt each
-// other's results: serialize them per device.
+// each call clears, in stream order, everything a build expects to start
+// empty: the build counters and the error word, the radix sort's look-back
+// words and the tree's arrival slots for this call's size. Nothing carries
+// over from one call to the next, so a call's result depends only on its own
+// inputs. Calls whose work overlaps on the GPU -- two streams, or two host
+// threads -- race on the array and corrupt each other's results: serialize
+// them per device.
 //
 // Set-up: the first call on each device looks the array's device address up
 // with cudaGetSymbolAddress (the array's name in host code is only a host-side
-// stand-in, not a device address). Make that first call before capturing
-// any stream.
+// stand-in, not a device address) and keeps it for the life of the process.
+// Make that first call before capturing any stream. A cudaDeviceReset ends
+// the context that address belongs to: do not call this entry point on that
+// device again in the same process.
 #include "../../include/lbvh_gb300.h"
 
 #include "build.cuh"
@@ -65,11 +70,15 @@ struct DeviceSlot
   cudaError_t setup_error = cudaSuccess;
   unsigned char* scratch = nullptr; // device address of g_noalloc_scratch
   int num_sms = 1;
-  uint32_t epoch = 0;               // epoch of the last call (look-back words, slots)
 };
 
 DeviceSlot g_slots[kMaxDevices];
-std::mutex g_epoch_mutex;
+
+// Tag of the look-back words (kEpoch + pass) and arrival slots (kEpoch) of
+// every call. Both are cleared at the start of each call, so a fixed tag
+// never meets a word left by an earlier call; it only has to differ from
+// the cleared value 0 and keep the sort's four passes apart.
+constexpr uint32_t kEpoch = 4;
 
 bool
 is_device_pointer(const void* p, int device)
@@ -118,15 +127,6 @@ lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint3
   if (slot.setup_error != cudaSuccess || !slot.scratch)
     return LBVH_ERR_DEVICE;
 
-  uint32_t epoch;
-  {
-    std::lock_guard<std::mutex> lock(g_epoch_mutex);
-    if (slot.epoch == 0 || slot.epoch > 0xfffffff0u)
-      slot.epoch = 4; // a wrapped counter would meet stale words: cleared below
-    epoch = slot.epoch;
-    slot.epoch += 4;
-  }
-
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   unsigned char* base = slot.scratch;
   const uint32_t nn = uint32_t(n);
@@ -150,21 +150,20 @@ lbvh_build_triangles_noalloc(const float* d_tris, size_t n, void* d_nodes, uint3
   const uint32_t mcap = uint32_t(slot.num_sms) * 8;
   b.morton_blocks = mwant < 1 ? 1 : (mwant > mcap ? mcap : mwant);
 
-  // What must start at zero: the bounds/sort counters and the error word.
-  // The look-back words and the tree's arrival slots carry the epoch of the
-  // call that wrote them and are cleared only when the epoch counter starts
-  // (or restarts after wrapping).
+  // What must start at zero, cleared by every call: the bounds/sort
+  // counters and the error word, the look-back words of this size's sort
+  // tiles, and the arrival slots of its n - 1 split positions.
   cudaError_t e = cudaMemsetAsync(b.state, 0, sizeof(BuildState), s);
-  if (e == cudaSuccess && epoch == 4)
-    e = cudaMemsetAsync(b.lookback, 0, kTiles * 256 * 8, s);
-  if (e == cudaSuccess && epoch == 4)
-    e = cudaMemsetAsync(b.slots, 0, 8 * kNoAllocMaxPrims, s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b.lookback, 0, sort_tiles(nn) * 256 * 8, s);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(b.slots, 0, 8 * size_t(nn - 1), s);
   if (e == cudaSuccess)
     e = launch_curve_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, s);
   if (e == cudaSuccess)
-    e = launch_sort(nn, false, epoch, b, s);
+    e = launch_sort(nn, false, kEpoch, b, s);
   if (e == cudaSuccess)
-    e = launch_fit_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, static_cast<Node*>(d_nodes), epoch, s);
+    e = launch_fit_tris(reinterpret_cast<const Tri*>(d_tris), nn, b, static_cast<Node*>(d_nodes), kEpoch, s);
   if (e == cudaSuccess && d_status)
     e = cudaMemcpyAsync(d_status, &b.state->error, 4, cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) {

@@ -6,8 +6,10 @@ ctypes access to two CPU implementations of the reference LBVH path
 * ``port``: ``liboracle.so``, our C++ restatement (``lbvh_oracle.cpp``). It is
   built on every machine, including the GPU host.
 * ``ref``: ``_ref/libref.so``, the unmodified reference header compiled through
-  ``ref_shim.cpp``. It only exists where the reference source tree was present
-  at build time, and is used to pin ``port`` and to make golden fixtures.
+  ``ref_shim.cpp``. It exists where the reference's files were present at
+  build time (a reference checkout, or the copy ``stage_ref.sh`` puts in
+  ``baseline/_ref``, which travels with the working tree), and is used to pin
+  ``port``, to make golden fixtures and as the timed CPU baseline.
 
 Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
 use this package, and only as the checker or as the timed CPU baseline.
@@ -43,9 +45,24 @@ _P = ctypes.c_void_p
 _S = ctypes.c_size_t
 
 
+STAGED_REF = os.path.join(os.path.dirname(HERE), "baseline", "_ref")
+
+
+def ref_dir() -> str:
+    """Where the reference's files are compiled from: $LBVH_REF_DIR, else the
+    staged copy in baseline/_ref (see stage_ref.sh)."""
+    return os.environ.get("LBVH_REF_DIR") or STAGED_REF
+
+
+def stage_reference() -> None:
+    """Copies the reference files libref.so needs into baseline/_ref where a
+    reference checkout is present (a no-op elsewhere)."""
+    subprocess.run(["sh", os.path.join(HERE, "stage_ref.sh")], check=True)
+
+
 def build_libs(ref_dir: str | None = None) -> None:
     """Runs oracle/Makefile (liboracle.so, plus _ref/libref.so when the
-    reference tree exists)."""
+    reference's files are present: $LBVH_REF_DIR or baseline/_ref)."""
     cmd = ["make", "-s", "-C", HERE]
     if ref_dir:
         cmd.append(f"REF_DIR={ref_dir}")
@@ -228,7 +245,8 @@ def port() -> Port:
 
 
 def ref() -> Ref | None:
-    """The reference itself, or None where it was not built (GPU host)."""
+    """The reference itself, or None where it was not built (no reference
+    files were staged on this machine)."""
     global _ref
     if _ref is None:
         path = os.path.join(HERE, "_ref", "libref.so")

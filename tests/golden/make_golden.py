@@ -1,7 +1,9 @@
 """Generates the golden fixtures in this folder from the UNMODIFIED reference.
 
-Run here, where the reference tree exists (it is not needed afterwards):
+Run where the reference's files are available (they are not needed
+afterwards):
 
+    sh oracle/stage_ref.sh [REF_SRC]    # copies them into baseline/_ref
     make -C oracle                      # builds oracle/_ref/libref.so
     python tests/golden/make_golden.py  # writes tests/golden/*.npz
 
@@ -24,7 +26,7 @@ import oracle  # noqa: E402
 from lbvh_gb300 import scenes  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.environ.get("LBVH_REF_DIR", "/root/reference")
+REF_DIR = oracle.ref_dir()  # $LBVH_REF_DIR, else the copy staged in baseline/_ref
 
 
 def edge_rays(tris: np.ndarray, nodes: np.ndarray, seed: int) -> np.ndarray:

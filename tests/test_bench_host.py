@@ -64,3 +64,55 @@ def test_trace_profile_figures_come_from_the_committed_capture():
     assert os.path.exists(os.path.join(ROOT, p["source"]))
     assert bench.measured_traffic("k_trace_tris", "dram_bytes_per_launch") > 0
     assert bench.measured_profile("no_such_kernel", ("l1_hit_rate",)) is None
+
+
+def test_room_config_is_identical_for_identical_rays():
+    """Both arms build the step's config from their own bounce rays; equal
+    rays give an equal config (the digest covers every ray of the step)."""
+    tris = scenes.soup(100, 1)
+    prim = scenes.pinhole_rays(8, 8)
+    bounce = prim[::2].copy()
+    a = bench.room_config(tris, prim, bounce, 1)
+    b = bench.room_config(tris.copy(), prim.copy(), bounce.copy(), 1)
+    assert a == b and a["rays_per_step"] == 96
+    bounce[0, 0] += 1.0
+    assert bench.room_config(tris, prim, bounce, 1)["rays_sha1"] != a["rays_sha1"]
+
+
+def test_final_line_stays_short():
+    """The final JSON line keeps the contract's keys and one-line summaries
+    of the extra sections, short enough to survive a log tail."""
+    import json
+
+    served = {"throughput_ratio": 6.5, "server": {"p99_ms": 36.5}, "plain": {"p99_ms": 290.7}, "results_equal": True}
+    line = {"metric": bench.METRIC, "value": 55.0, "unit": "Mrays/s", "n_gpus": 1, "steps": 20, "warmup": 5,
+            "ms_per_step": 75.3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": bench.room_config(scenes.soup(10, 1), scenes.pinhole_rays(4, 4),
+                                                             scenes.pinhole_rays(2, 2), 1),
+            "build": {"ms": 0.1, "mprims_s": 2000.0}, "trace": {"ms": 75.0, "mrays_s": 55.0,
+                                                                "primary_hit_fraction": 0.99},
+            "build_16m": {"ms": 1.03, "mprims_s": 15500.0, "refit_ms": 0.6, "triangles": 16000000,
+                          "roofline": {"frac": 0.6, "achieved": 4000.0}},
+            "config1": {"value": 3900.0, "ms_per_step": 0.53, "build_ms": 0.07, "trace_ms": 0.46, "workload": "t"},
+            "batched": {"graph_step_ms": 628.1, "plain_step_ms": 26441.0, "speedup_vs_plain": 42.1,
+                        "sorted_leaves": {"step_ms": 12.9}, "tuning": {"x": 1}},
+            "served": {"mix": served, "small": served},
+            "roofline": {"bound": "hbm", "kernel": "lbvh build, 16M-triangle soup (all build kernels)",
+                         "achieved": 4070.1, "peak": 6697.8, "unit": "GB/s", "frac": 0.6077, "bytes_per_prim": 264,
+                         "traffic": 2762219008, "traffic_scope": "DRAM bytes of one whole build (all kernels), ncu",
+                         "peak_kind": "measured"},
+            "trace_profile": {"issue_slots_busy": 0.7, "simt_threads_per_instruction": 16.0, "l1_hit_rate": 0.8,
+                              "l2_hit_rate": 0.9, "warps_active_of_max": 0.45, "source": "profiles/x.md"},
+            "cpu_baseline": {"value": 0.6, "unit": "Mrays/s", "cores": 16, "kind": "reference",
+                             "lib": "oracle/_ref/libref.so", "sample": "build of all 262267 triangles + every 16th "
+                                                                       "primary and bounce ray (258858) per step, 3 steps"},
+            "e2e": {"value": 50.0, "unit": "Mrays/s", "ms_per_step": 80.0, "h2d_bytes_per_step": 145125000,
+                    "d2h_bytes_per_step": 66267664, "transfer": "triangles copied; rays read and hits written in "
+                                                                "place in page-locked host memory"},
+            "gpu_launches": 220, "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": [], "samples": 10}}
+    out = bench.summary_line(line)
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks"):
+        assert k in out, k
+    assert out["served"]["small"]["ratio"] == 6.5 and out["build_16m"]["frac"] == 0.6
+    assert len(json.dumps(out)) < 3000

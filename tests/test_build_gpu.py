@@ -150,6 +150,35 @@ def test_invalid_arguments_raise(ctx):
         lb.Builder(ctx)(np.zeros((4, 12), np.float64))
 
 
+@pytest.mark.parametrize("sorted_leaves", [False, True])
+def test_lookback_wait_that_runs_out_reports_timeout(lib_built, port, sorted_leaves):
+    """A radix-sort look-back wait that never sees its word gives up after
+    the spin limit: the kernel returns, the build reports LBVH_ERR_TIMEOUT
+    (no tree is built over the unsorted codes), and the same context then
+    builds exactly again. The stall parameter makes every wait look for a
+    tag no tile writes -- a flag that nothing sets."""
+    from lbvh_gb300 import _lib
+
+    c = lb.Context()
+    t = scenes.soup(60_000, seed=81)
+    c.set_param(_lib.PARAM_LOOKBACK_SPIN_LIMIT, 512)
+    c.set_param(_lib.PARAM_TEST_LOOKBACK_STALL, 1)
+    with pytest.raises(lb.LbvhError) as e:
+        lb.Builder(c, sorted_leaves=sorted_leaves)(t)  # host input: the call returns finished
+    assert e.value.status == _lib.LBVH_ERR_TIMEOUT
+    c.set_param(_lib.PARAM_TEST_LOOKBACK_STALL, 0)
+    with pytest.raises(ValueError):
+        c.set_param(_lib.PARAM_LOOKBACK_SPIN_LIMIT, 0)
+    c.set_param(_lib.PARAM_LOOKBACK_SPIN_LIMIT, 1 << 22)
+    got = lb.Builder(c, sorted_leaves=sorted_leaves)(dev(t))
+    c.synchronize()
+    if sorted_leaves:
+        perm = port.curve(t, 16)[2]
+        assert nodes_equal(got.nodes(), port.build(t[perm], 16))
+    else:
+        assert nodes_equal(got.nodes(), port.build(t, 16))
+
+
 def test_full_size_16m_build_parity(ctx, port):
     """The 16M-triangle random soup (the roofline workload) against the
     oracle, bit for bit, plus the reference's structural invariants."""

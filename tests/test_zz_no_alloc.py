@@ -29,16 +29,18 @@ def _noalloc(tris, nodes, status, stream):
         ctypes.c_void_p(stream))
 
 
-def test_noalloc_build_matches_allocating_build(lib_built):
+def test_noalloc_build_matches_allocating_build(lib_built, port):
     assert torch.cuda.is_available(), "GPU tests need CUDA"
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev).cuda_stream
     ctx = lb.Context(0, stream)
     status = torch.full((1,), 0xFFFF, dtype=torch.int32, device=dev)
-    # two calls in a row with different sizes: the second reuses (and must
-    # fully reset) the scratch the first one left behind
-    for n, seed in [(_lib.NOALLOC_MAX_PRIMS, 71), (3_001, 72), (2, 73)]:
-        tris = torch.from_numpy(scenes.soup(n, seed)).to(dev)
+    # calls in a row: two full-size soups (the tree's global phase and its
+    # arrival slots run at this size), then smaller ones; each call reuses
+    # (and must fully reset) the scratch the previous one left behind
+    for n, seed in [(_lib.NOALLOC_MAX_PRIMS, 71), (_lib.NOALLOC_MAX_PRIMS, 74), (3_001, 72), (2, 73)]:
+        tris_h = scenes.soup(n, seed)
+        tris = torch.from_numpy(tris_h).to(dev)
         nodes = torch.empty(((n - 1) * 8,), dtype=torch.int32, device=dev)
         status.fill_(0xFFFF)
         assert _noalloc(tris, nodes, status, stream) == _lib.LBVH_OK
@@ -47,6 +49,20 @@ def test_noalloc_build_matches_allocating_build(lib_built):
         want = lb.Builder(ctx)(tris).nodes()  # the allocating entry point
         got = nodes.cpu().numpy().view(lb.NODE_DTYPE)
         assert got.tobytes() == want.tobytes(), n  # build parity is bit-exact
+        assert got.tobytes() == port.build(tris_h, 8).tobytes(), n  # and equal to the oracle
+
+
+def test_noalloc_without_status_word(lib_built, port):
+    """d_status may be NULL: the build still runs and is still exact."""
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for n, seed in [(50_000, 75), (50_000, 76)]:
+        tris_h = scenes.soup(n, seed)
+        tris = torch.from_numpy(tris_h).to(dev)
+        nodes = torch.empty(((n - 1) * 8,), dtype=torch.int32, device=dev)
+        assert _noalloc(tris, nodes, None, stream) == _lib.LBVH_OK
+        torch.cuda.synchronize()
+        assert nodes.cpu().numpy().view(lb.NODE_DTYPE).tobytes() == port.build(tris_h, 8).tobytes(), seed
 
 
 def test_noalloc_rejects_what_it_cannot_serve(lib_built):
