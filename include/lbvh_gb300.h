@@ -54,7 +54,9 @@ typedef enum lbvh_status
   LBVH_ERR_DEVICE = 4,      /* CUDA runtime error; see lbvh_ctx_last_error */
   LBVH_ERR_BAD_TOPOLOGY = 5, /* a node array that is not a binary tree */
   LBVH_ERR_NOT_RESIDENT = 6, /* server: a trace or refit of a scene it does not hold */
-  LBVH_ERR_BUDGET = 7        /* server: a build larger than the whole HBM budget */
+  LBVH_ERR_BUDGET = 7,       /* server: a build larger than the whole HBM budget */
+  LBVH_ERR_CANCELLED = 8,    /* server: cancelled (lbvh_server_cancel) before it started */
+  LBVH_ERR_EXPIRED = 9       /* server: still queued after the server's max_queue_s */
 } lbvh_status;
 
 typedef struct lbvh_ctx lbvh_ctx; /* device, stream, workspace */
@@ -128,6 +130,8 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             place, each warp's batch of 32 as one 512-byte store (the
                                             traversal then reaches host memory over the CPU-GPU link);
                                             pageable host memory is always copied */
+#define LBVH_PARAM_TRACE_SHORT_STACK 8   /* traversal stack entries per ray kept in shared memory (the
+                                            rest in local memory): 0, 8 or 16 */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */
@@ -337,6 +341,8 @@ typedef struct lbvh_server_config
   size_t batch_max_requests;   /* most requests in one coalesced launch */
   size_t trace_batch_max_rays; /* largest trace that is coalesced */
   size_t host_budget;          /* bytes of host memory for evicted scenes (0: evicted scenes are dropped) */
+  double max_queue_s;          /* a request not started this many seconds after its arrival fails with
+                                  LBVH_ERR_EXPIRED (0: requests wait as long as they must) */
 } lbvh_server_config;
 
 typedef struct lbvh_request_done
@@ -357,6 +363,7 @@ typedef struct lbvh_server_stats
   uint64_t resident_scenes, resident_bytes;
   uint64_t spills, reloads;        /* evictions kept on the host; scenes loaded back */
   uint64_t spilled_scenes, spilled_bytes;
+  uint64_t cancelled, expired;     /* requests that never ran: lbvh_server_cancel, max_queue_s */
 } lbvh_server_stats;
 
 LBVH_API int lbvh_server_create(const lbvh_server_config* config, lbvh_server** out);
@@ -372,6 +379,17 @@ LBVH_API int lbvh_server_wait_any(lbvh_server* server, lbvh_request_done* out, s
 /* The server's clock: seconds since it was created (the clock of
  * lbvh_request_done's times). */
 LBVH_API double lbvh_server_clock(const lbvh_server* server);
+/* Cancels a request that has not started: it is reported done with
+ * LBVH_ERR_CANCELLED and never runs (later requests of its scene run as if it
+ * had not been submitted). A request that has started or finished is not
+ * affected. Returns LBVH_OK either way; the outcome is the request's report. */
+LBVH_API int lbvh_server_cancel(lbvh_server* server, uint64_t ticket);
+/* Test hook (failure injection on the host): the next `count` device
+ * allocations the server's workers make for request data (triangles, node
+ * and ray/hit staging buffers) fail as on an exhausted device. Each affected
+ * request reports LBVH_ERR_OOM, the HBM budget it held is returned, a scene
+ * whose rebuild failed keeps its previous tree, and the server goes on. */
+LBVH_API int lbvh_server_inject_alloc_failures(lbvh_server* server, uint32_t count);
 /* Blocks until every request submitted so far has finished. */
 LBVH_API int lbvh_server_drain(lbvh_server* server);
 LBVH_API int lbvh_server_stats_get(lbvh_server* server, lbvh_server_stats* out);

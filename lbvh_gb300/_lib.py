@@ -21,6 +21,8 @@ LBVH_ERR_DEVICE = 4
 LBVH_ERR_BAD_TOPOLOGY = 5
 LBVH_ERR_NOT_RESIDENT = 6
 LBVH_ERR_BUDGET = 7
+LBVH_ERR_CANCELLED = 8
+LBVH_ERR_EXPIRED = 9
 
 REQ_BUILD, REQ_REFIT, REQ_TRACE = 0, 1, 2
 
@@ -32,6 +34,7 @@ PARAM_TRACE_CHUNK = 4
 PARAM_TRACE_IN_PLACE = 5
 PARAM_LOOKBACK_SPIN_LIMIT = 6
 PARAM_TEST_LOOKBACK_STALL = 7
+PARAM_TRACE_SHORT_STACK = 8
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000
@@ -84,6 +87,8 @@ SIGNATURES = {
     "lbvh_server_submit": (_I, [_P, _I, ctypes.c_int64, _P, _S, _P, ctypes.POINTER(ctypes.c_uint64)]),
     "lbvh_server_wait_any": (_I, [_P, _P, _S, ctypes.c_double, ctypes.POINTER(_S)]),
     "lbvh_server_drain": (_I, [_P]),
+    "lbvh_server_cancel": (_I, [_P, ctypes.c_uint64]),
+    "lbvh_server_inject_alloc_failures": (_I, [_P, _U32]),
     "lbvh_server_clock": (ctypes.c_double, [_P]),
     "lbvh_server_stats_get": (_I, [_P, _P]),
     "lbvh_server_resident": (_I, [_P, _P, _S, ctypes.POINTER(_S)]),
@@ -94,7 +99,8 @@ SIGNATURES = {
 class ServerConfig(ctypes.Structure):
     """lbvh_server_config"""
     _fields_ = [("device", _I), ("slots", _I), ("hbm_budget", _S), ("batch_max_tris", _S),
-                ("batch_max_requests", _S), ("trace_batch_max_rays", _S), ("host_budget", _S)]
+                ("batch_max_requests", _S), ("trace_batch_max_rays", _S), ("host_budget", _S),
+                ("max_queue_s", ctypes.c_double)]
 
 
 class RequestDone(ctypes.Structure):
@@ -110,7 +116,8 @@ class ServerStats(ctypes.Structure):
                 ("coalesced_requests", ctypes.c_uint64), ("evictions", ctypes.c_uint64),
                 ("resident_scenes", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64),
                 ("spills", ctypes.c_uint64), ("reloads", ctypes.c_uint64),
-                ("spilled_scenes", ctypes.c_uint64), ("spilled_bytes", ctypes.c_uint64)]
+                ("spilled_scenes", ctypes.c_uint64), ("spilled_bytes", ctypes.c_uint64),
+                ("cancelled", ctypes.c_uint64), ("expired", ctypes.c_uint64)]
 
 
 class LbvhError(RuntimeError):

@@ -504,6 +504,10 @@ lbvh_status_string(int s)
       return "scene not resident";
     case LBVH_ERR_BUDGET:
       return "larger than the HBM budget";
+    case LBVH_ERR_CANCELLED:
+      return "cancelled";
+    case LBVH_ERR_EXPIRED:
+      return "expired in the queue";
     default:
       return "unknown status";
   }
@@ -646,6 +650,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
       if (value < 0 || value > 2)
         return fail(c, LBVH_ERR_INVALID_ARG, "trace in-place mode %d outside [0, 2]", value);
       c->trace_in_place = value;
+      return LBVH_OK;
+    case LBVH_PARAM_TRACE_SHORT_STACK:
+      if (value != 0 && value != 8 && value != 16)
+        return fail(c, LBVH_ERR_INVALID_ARG, "short stack %d is not 0, 8 or 16", value);
+      c->trace.short_stack = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
       if (value < 1 || value > (1 << 24))

@@ -139,6 +139,7 @@ struct Worker
   size_t rays_cap = 0;
   void* hits = nullptr;
   size_t hits_cap = 0;
+  std::atomic<uint32_t>* fail_allocs = nullptr; // the server's injected allocation failures
 };
 
 } // namespace
@@ -157,8 +158,11 @@ struct lbvh_server
   uint64_t next_ticket = 1, next_seq = 0, submitted = 0, completed = 0;
   uint64_t coalesced = 0, evictions = 0, used_snapshot = 0;
   uint64_t spills = 0, reloads = 0, spilled_snapshot = 0, host_used_snapshot = 0;
+  uint64_t cancelled = 0, expired = 0;
   std::deque<JobPtr> spill_jobs; // for the spill thread
+  std::vector<uint64_t> cancels; // tickets to cancel if still queued
   bool dirty = false, stop = false;
+  std::atomic<uint32_t> fail_allocs{ 0 }; // injected allocation failures still to come
   // dispatch thread only
   std::unordered_map<int64_t, std::deque<ReqPtr>> queues;
   std::unordered_map<int64_t, ResPtr> resident;
@@ -229,6 +233,22 @@ cuda_ok(Job& j, cudaError_t e, const char* what)
   return false;
 }
 
+// A worker's device allocation for request data. An injected failure
+// (lbvh_server_inject_alloc_failures) is reported exactly as cudaMallocAsync
+// reports an exhausted device.
+cudaError_t
+worker_malloc(Worker& w, void** p, size_t bytes)
+{
+  if (w.fail_allocs) {
+    uint32_t k = w.fail_allocs->load();
+    while (k > 0 && !w.fail_allocs->compare_exchange_weak(k, k - 1)) {
+    }
+    if (k > 0)
+      return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocAsync(p, bytes, w.stream);
+}
+
 #define W_CK(call, what)                                                                                               \
   do {                                                                                                                 \
     if (!cuda_ok(j, (call), what))                                                                                     \
@@ -251,7 +271,7 @@ grow(Job& j, Worker& w, void*& buf, size_t& cap, size_t bytes)
   buf = nullptr;
   cap = 0;
   const size_t want = std::max(bytes, size_t(1) << 20);
-  W_CK(cudaMallocAsync(&buf, want, w.stream), "staging allocation");
+  W_CK(worker_malloc(w, &buf, want), "staging allocation");
   cap = want;
   return true;
 }
@@ -260,7 +280,7 @@ bool
 run_build(Worker& w, Job& j)
 {
   const Request& r = *j.group[0];
-  W_CK(cudaMallocAsync(&j.tris, kTriBytes * r.rows, w.stream), "triangle allocation");
+  W_CK(worker_malloc(w, &j.tris, kTriBytes * r.rows), "triangle allocation");
   W_CK(cudaMemcpyAsync(j.tris, r.data, kTriBytes * r.rows, cudaMemcpyDefault, w.stream), "triangle upload");
   W_LB(lbvh_bvh_create(w.ctx, &j.bvh), "bvh create");
   W_LB(lbvh_build_triangles(w.ctx, static_cast<const float*>(j.tris), r.rows, 0, j.bvh), "build");
@@ -274,7 +294,7 @@ bool
 run_batch_build(Worker& w, Job& j)
 {
   const size_t total = j.off.back();
-  W_CK(cudaMallocAsync(&j.tris, kTriBytes * total, w.stream), "triangle allocation");
+  W_CK(worker_malloc(w, &j.tris, kTriBytes * total), "triangle allocation");
   for (size_t k = 0; k < j.group.size(); k++)
     W_CK(cudaMemcpyAsync(static_cast<char*>(j.tris) + kTriBytes * j.off[k], j.group[k]->data,
                          kTriBytes * j.group[k]->rows, cudaMemcpyDefault, w.stream),
@@ -298,7 +318,7 @@ run_refit(Worker& w, Job& j)
     const size_t n = b.off[k + 1] - b.off[k];
     W_LB(lbvh_bvh_create(w.ctx, &j.bvh), "bvh create");
     void* nodes = nullptr;
-    W_CK(cudaMallocAsync(&nodes, kNodeBytes * (n - 1), w.stream), "node allocation");
+    W_CK(worker_malloc(w, &nodes, kNodeBytes * (n - 1)), "node allocation");
     const float* mesh = reinterpret_cast<const float*>(static_cast<const char*>(b.tris) + kTriBytes * b.off[k]);
     int st = lbvh_batch_mesh_nodes(w.ctx, b.batch, k, nodes);
     if (st == LBVH_OK)
@@ -307,7 +327,7 @@ run_refit(Worker& w, Job& j)
     W_LB(st, "batch member import");
     bvh = j.bvh;
   }
-  W_CK(cudaMallocAsync(&j.tris, kTriBytes * r.rows, w.stream), "triangle allocation");
+  W_CK(worker_malloc(w, &j.tris, kTriBytes * r.rows), "triangle allocation");
   W_CK(cudaMemcpyAsync(j.tris, r.data, kTriBytes * r.rows, cudaMemcpyDefault, w.stream), "triangle upload");
   W_LB(lbvh_refit_triangles(w.ctx, bvh, static_cast<const float*>(j.tris)), "refit");
   W_LB(lbvh_bvh_prepare_trace(w.ctx, bvh), "prepare trace");
@@ -981,6 +1001,72 @@ unblock(lbvh_server* s)
              std::to_string(s->cfg.hbm_budget) + " bytes");
 }
 
+// Cancelled requests that have not started leave their queues and are
+// reported; a ticket that is not queued (started, finished, unknown) is
+// ignored.
+void
+cancel_queued(lbvh_server* s, const std::vector<uint64_t>& tickets)
+{
+  std::unordered_set<uint64_t> want(tickets.begin(), tickets.end());
+  uint64_t k = 0;
+  const double t = s->now();
+  for (auto it = s->queues.begin(); it != s->queues.end();) {
+    auto& q = it->second;
+    for (auto r = q.begin(); r != q.end();) {
+      if (want.count((*r)->ticket)) {
+        complete(s, *r, LBVH_ERR_CANCELLED, "cancelled before it started", t);
+        r = q.erase(r);
+        k++;
+      } else {
+        ++r;
+      }
+    }
+    it = q.empty() ? s->queues.erase(it) : std::next(it);
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->cancelled += k;
+}
+
+// Requests still queued max_queue_s after their arrival fail. Queues are in
+// arrival order, so only their fronts are looked at.
+void
+expire_queued(lbvh_server* s)
+{
+  if (s->cfg.max_queue_s <= 0)
+    return;
+  const double t = s->now();
+  uint64_t k = 0;
+  for (auto it = s->queues.begin(); it != s->queues.end();) {
+    auto& q = it->second;
+    while (!q.empty() && q.front()->arrival + s->cfg.max_queue_s <= t) {
+      complete(s, q.front(), LBVH_ERR_EXPIRED,
+               "not started within " + std::to_string(s->cfg.max_queue_s) + " s of its arrival", t);
+      q.pop_front();
+      k++;
+    }
+    it = q.empty() ? s->queues.erase(it) : std::next(it);
+  }
+  if (k) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->expired += k;
+  }
+}
+
+// When the next queued request expires (server clock), or a negative value.
+double
+next_expiry(const lbvh_server* s)
+{
+  if (s->cfg.max_queue_s <= 0 || s->queues.empty())
+    return -1.0;
+  double t = -1.0;
+  for (const auto& kv : s->queues) {
+    const double e = kv.second.front()->arrival + s->cfg.max_queue_s;
+    if (t < 0 || e < t)
+      t = e;
+  }
+  return t;
+}
+
 void
 dispatcher_loop(lbvh_server* s)
 {
@@ -988,6 +1074,7 @@ dispatcher_loop(lbvh_server* s)
   for (;;) {
     std::vector<ReqPtr> inbox;
     std::vector<JobPtr> fin;
+    std::vector<uint64_t> cancels;
     {
       std::unique_lock<std::mutex> lk(s->mu);
       while (!s->dirty) {
@@ -1002,14 +1089,24 @@ dispatcher_loop(lbvh_server* s)
           }
           return;
         }
-        s->cv_dispatch.wait(lk);
+        const double e = next_expiry(s); // queues are the dispatcher's own
+        if (e < 0) {
+          s->cv_dispatch.wait(lk);
+        } else if (s->cv_dispatch.wait_for(lk, std::chrono::duration<double>(std::max(0.0, e - s->now()))) ==
+                   std::cv_status::timeout) {
+          s->dirty = true; // a queued request has expired
+        }
       }
       s->dirty = false;
       inbox.swap(s->inbox);
       fin.swap(s->finished);
+      cancels.swap(s->cancels);
     }
     for (ReqPtr& r : inbox)
       s->queues[r->scene].push_back(std::move(r));
+    if (!cancels.empty())
+      cancel_queued(s, cancels);
+    expire_queued(s);
     for (JobPtr& j : fin) {
       if (j->worker) // spill jobs run on the spill thread
         j->worker->busy = false;
@@ -1093,7 +1190,7 @@ lbvh_server_create(const lbvh_server_config* cfg, lbvh_server** out)
   if (!cfg || !out)
     return LBVH_ERR_INVALID_ARG;
   *out = nullptr;
-  if (cfg->slots < 1 || cfg->slots > 64 || cfg->hbm_budget == 0)
+  if (cfg->slots < 1 || cfg->slots > 64 || cfg->hbm_budget == 0 || !(cfg->max_queue_s >= 0))
     return LBVH_ERR_INVALID_ARG;
   if (cudaSetDevice(cfg->device) != cudaSuccess)
     return LBVH_ERR_DEVICE;
@@ -1112,6 +1209,7 @@ lbvh_server_create(const lbvh_server_config* cfg, lbvh_server** out)
     for (int k = 0; k < cfg->slots; k++) {
       auto w = std::make_unique<Worker>();
       w->index = k;
+      w->fail_allocs = &s->fail_allocs;
       if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
           lbvh_ctx_create(cfg->device, w->stream, &w->ctx) != LBVH_OK) {
         s->workers.push_back(std::move(w));
@@ -1189,6 +1287,27 @@ lbvh_server_submit(lbvh_server* s, int kind, int64_t scene, const float* data, s
 }
 
 int
+lbvh_server_cancel(lbvh_server* s, uint64_t ticket)
+{
+  if (!s)
+    return LBVH_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->cancels.push_back(ticket);
+  s->dirty = true;
+  s->cv_dispatch.notify_one();
+  return LBVH_OK;
+}
+
+int
+lbvh_server_inject_alloc_failures(lbvh_server* s, uint32_t count)
+{
+  if (!s)
+    return LBVH_ERR_INVALID_ARG;
+  s->fail_allocs.store(count);
+  return LBVH_OK;
+}
+
+int
 lbvh_server_wait_any(lbvh_server* s, lbvh_request_done* out, size_t max, double timeout_s, size_t* n_out)
 {
   if (!s || !out || !n_out || max == 0)
@@ -1237,6 +1356,8 @@ lbvh_server_stats_get(lbvh_server* s, lbvh_server_stats* out)
   out->reloads = s->reloads;
   out->spilled_scenes = s->spilled_snapshot;
   out->spilled_bytes = s->host_used_snapshot;
+  out->cancelled = s->cancelled;
+  out->expired = s->expired;
   return LBVH_OK;
 }
 

@@ -170,7 +170,12 @@ k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict_
 constexpr uint32_t kHitRing = 4;
 constexpr uint32_t kHitDirect = kHitRing; // a ray whose hit is written directly
 
-template<bool kCounts, bool kBatch, bool kHostHits = false>
+// kShort > 0: the top kShort entries of each lane's stack live in shared
+// memory (a ring indexed by the logical stack position), the rest in local
+// memory; a push onto a full ring moves the ring's bottom entry to local
+// memory first, a pop from an empty ring reads local memory. The logical
+// stack, its 128-entry capacity and its drop rule are unchanged.
+template<bool kCounts, bool kBatch, bool kHostHits = false, int kShort = 0>
 __global__ __launch_bounds__(kTraceThreads, 8) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
@@ -198,6 +203,8 @@ k_trace(const WideNode* __restrict__ wnodes,
   // reference's would.
   uint2 stack[kStackSize];
   uint32_t sp = 0;
+  uint32_t lo = 0; // kShort: entries [lo, sp) are in the shared ring, [0, lo) in local memory
+  __shared__ uint2 s_stack[kShort > 0 ? kShort : 1][kTraceThreads];
   uint2 cur = make_uint2(0u, 0u);
   bool has_cur = false;
   uint32_t ray = kMiss; // ray index of this lane, kMiss = none
@@ -318,6 +325,7 @@ k_trace(const WideNode* __restrict__ wnodes,
             nb = tb - lo;
           }
             sp = 0;
+            lo = 0;
             cur = make_uint2(0u, __float_as_uint(inf)); // root, pushed with +inf
             has_cur = true;
             best_p = kMiss;
@@ -372,8 +380,18 @@ k_trace(const WideNode* __restrict__ wnodes,
         const bool lfirst = lt < rt; // left nearer: push right, then left
         const uint2 far = lfirst ? make_uint2(right, __float_as_uint(rt)) : make_uint2(left, __float_as_uint(lt));
         const uint2 near = lfirst ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
-        if (sp < kStackSize)
-          stack[sp++] = far;
+        if (sp < kStackSize) {
+          if (kShort > 0) {
+            if (sp - lo == uint32_t(kShort)) { // ring full: its bottom entry moves to local memory
+              stack[lo] = s_stack[lo % kShort][threadIdx.x];
+              lo++;
+            }
+            s_stack[sp % kShort][threadIdx.x] = far;
+            sp++;
+          } else {
+            stack[sp++] = far;
+          }
+        }
         if (sp < kStackSize) {
           cur = near;
           has_cur = true;
@@ -390,7 +408,17 @@ k_trace(const WideNode* __restrict__ wnodes,
       if (!has_cur) {
         if (sp == 0)
           break;
-        cur = stack[--sp];
+        if (kShort > 0) {
+          if (sp == lo) { // the ring is empty: the entry is in local memory
+            cur = stack[--sp];
+            lo = sp;
+          } else {
+            --sp;
+            cur = s_stack[sp % kShort][threadIdx.x];
+          }
+        } else {
+          cur = stack[--sp];
+        }
       }
       has_cur = !(best_t < __uint_as_float(cur.y));
       if (has_cur)
@@ -456,16 +484,36 @@ launch_trace_tris(const WideNode* wnodes,
   const uint32_t blocks = want < cap ? want : cap;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + n_nodes);
-  if (n_box && n_tri)
-    k_trace<true, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri,
-                                                          ray_counter, wide, p.refill, nullptr, nullptr, 0);
-  else if (host_hits)
-    k_trace<false, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
-                                                                 nullptr, ray_counter, wide, p.refill, nullptr,
-                                                                 nullptr, 0);
-  else
-    k_trace<false, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
-                                                           ray_counter, wide, p.refill, nullptr, nullptr, 0);
+  auto go = [&](auto kernel, uint32_t* nb, uint32_t* nt) {
+    kernel<<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nb, nt, ray_counter, wide, p.refill,
+                                           nullptr, nullptr, 0);
+  };
+  const bool counts = n_box && n_tri;
+  switch (p.short_stack) {
+    case 8:
+      if (counts)
+        go(k_trace<true, false, false, 8>, n_box, n_tri);
+      else if (host_hits)
+        go(k_trace<false, false, true, 8>, nullptr, nullptr);
+      else
+        go(k_trace<false, false, false, 8>, nullptr, nullptr);
+      break;
+    case 16:
+      if (counts)
+        go(k_trace<true, false, false, 16>, n_box, n_tri);
+      else if (host_hits)
+        go(k_trace<false, false, true, 16>, nullptr, nullptr);
+      else
+        go(k_trace<false, false, false, 16>, nullptr, nullptr);
+      break;
+    default:
+      if (counts)
+        go(k_trace<true, false>, n_box, n_tri);
+      else if (host_hits)
+        go(k_trace<false, false, true>, nullptr, nullptr);
+      else
+        go(k_trace<false, false>, nullptr, nullptr);
+  }
   return cudaGetLastError();
 }
 

@@ -38,13 +38,20 @@ arithmetic is bit-identical to the reference.
 Latency = completion of the request's GPU work and result copy, as seen by
 the worker that ran it, minus arrival (submit) time, both on the server's
 clock.
+
+Failures stay on the host and leave the server serving: a request cancelled
+before it started (`cancel`) raises CancelledError, one still queued
+`max_queue_s` after its arrival raises TimeoutError, a device allocation that
+fails raises MemoryError (a rebuild that fails keeps the scene's previous
+tree), and `inject_alloc_failures` makes the next allocations fail on purpose
+so that tests can exercise that path.
 """
 from __future__ import annotations
 
 import ctypes
 import threading
 import time
-from concurrent.futures import Future
+from concurrent.futures import CancelledError, Future
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -79,8 +86,12 @@ def _exception(status: int, msg: str) -> BaseException:
         return KeyError(msg)
     if status == _lib.LBVH_ERR_INVALID_ARG:
         return ValueError(msg)
-    if status == _lib.LBVH_ERR_BUDGET:
+    if status in (_lib.LBVH_ERR_BUDGET, _lib.LBVH_ERR_OOM):
         return MemoryError(msg)
+    if status == _lib.LBVH_ERR_CANCELLED:
+        return CancelledError(msg)
+    if status == _lib.LBVH_ERR_EXPIRED:
+        return TimeoutError(msg)
     return _lib.LbvhError(status, msg)
 
 
@@ -90,10 +101,11 @@ class Server:
 
     def __init__(self, device: int = 0, slots: int = 4, hbm_budget: int = 120 << 30,
                  batch_max_tris: int = 65536, batch_max_requests: int = 128,
-                 trace_batch_max_rays: int = 1 << 16, host_budget: int = 64 << 30):
+                 trace_batch_max_rays: int = 1 << 16, host_budget: int = 64 << 30, max_queue_s: float = 0.0):
         L = _lib.lib()
         cfg = _lib.ServerConfig(int(device), int(slots), int(hbm_budget), int(batch_max_tris),
-                                int(batch_max_requests), int(trace_batch_max_rays), int(host_budget))
+                                int(batch_max_requests), int(trace_batch_max_rays), int(host_budget),
+                                float(max_queue_s))
         h = ctypes.c_void_p()
         st = L.lbvh_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if st:
@@ -132,7 +144,19 @@ class Server:
             if st:
                 raise _exception(st, "request rejected")
             self._waiting[ticket.value] = r  # keeps data and hits alive until done
+        r.future.ticket = ticket.value
         return r.future
+
+    def cancel(self, future: Future) -> None:
+        """Cancels the request behind `future` if it has not started (its
+        result then raises CancelledError); a started request finishes."""
+        _lib.lib().lbvh_server_cancel(self._h, future.ticket)
+
+    def inject_alloc_failures(self, count: int) -> None:
+        """Test hook: the next `count` device allocations of the server's
+        workers fail as on an exhausted device (those requests raise
+        MemoryError)."""
+        _lib.lib().lbvh_server_inject_alloc_failures(self._h, int(count))
 
     def close(self, wait: bool = True) -> None:
         """Finishes every submitted request, then frees the server."""
@@ -181,6 +205,14 @@ class Server:
     @property
     def spilled(self) -> int:
         return int(self._stats().spilled_scenes)
+
+    @property
+    def cancelled(self) -> int:
+        return int(self._stats().cancelled)
+
+    @property
+    def expired(self) -> int:
+        return int(self._stats().expired)
 
     @property
     def used(self) -> int:

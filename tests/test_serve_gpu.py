@@ -147,3 +147,93 @@ def test_page_locked_request_buffers(lib_built):
     finally:
         for a in (reg, reg_hits):
             cudart.cudaHostUnregister(a.ctypes.data)
+
+
+def test_injected_allocation_failures(lib_built):
+    """Allocation failures injected on the host: the failing requests raise
+    MemoryError, the HBM budget they held comes back, a scene whose rebuild
+    failed keeps its previous tree, and the server goes on serving with the
+    plain path's results."""
+    t1, t2 = scenes.soup(30_000, 91), scenes.soup(30_000, 92)
+    rays = scenes.incoherent_rays(t1, 4_000, 93)
+    with Server(slots=2, batch_max_tris=0) as srv:
+        srv.submit("build", 1, t1).result(timeout=60)
+        before = srv.submit("trace", 1, rays).result(timeout=60)
+        used = srv.used
+        srv.inject_alloc_failures(1)
+        with pytest.raises(MemoryError):
+            srv.submit("build", 1, t2).result(timeout=60)  # the rebuild fails ...
+        assert srv.used == used
+        kept = srv.submit("trace", 1, rays).result(timeout=60)  # ... and the old tree stays
+        assert hit_mismatches(kept, before).size == 0
+        srv.inject_alloc_failures(1)
+        with pytest.raises(MemoryError):
+            srv.submit("build", 2, t2).result(timeout=60)
+        assert srv.used == used and 2 not in srv.resident
+        with pytest.raises(KeyError):
+            srv.submit("trace", 2, rays).result(timeout=60)
+        srv.submit("build", 2, t2).result(timeout=60)  # nothing injected any more
+        got = srv.submit("trace", 2, rays).result(timeout=60)
+    want = run_plain([(0.0, "build", 2, t2), (0.0, "trace", 2, rays)])[1][0]
+    assert hit_mismatches(got, want).size == 0
+
+
+def test_injected_failure_of_a_coalesced_build(lib_built):
+    """Small builds coalesced into one batched build share one allocation:
+    an injected failure fails those requests only; the others are built."""
+    meshes = [scenes.soup(2_000 + 100 * k, 100 + k) for k in range(6)]
+    with Server(slots=1) as srv:
+        srv.inject_alloc_failures(1)
+        futs = [srv.submit("build", k, m) for k, m in enumerate(meshes)]
+        failed = []
+        for k, f in enumerate(futs):
+            try:
+                f.result(timeout=60)
+            except MemoryError:
+                failed.append(k)
+        assert failed  # the first allocation failed
+        assert sorted(srv.resident) == [k for k in range(6) if k not in failed]
+        assert srv.used == sum(scene_bytes(meshes[k].shape[0]) for k in srv.resident)
+        for k in failed:  # a later build of the same scene succeeds
+            srv.submit("build", k, meshes[k]).result(timeout=60)
+        assert sorted(srv.resident) == list(range(6))
+
+
+def test_cancelled_request_never_runs(lib_built):
+    """A trace queued behind a long rebuild of its scene is cancelled before
+    it starts: it raises CancelledError, the next trace runs normally."""
+    from concurrent.futures import CancelledError
+
+    big = scenes.soup_large(4_000_000, 94)
+    rays = scenes.incoherent_rays(big, 2_000, 95)
+    with Server(slots=1) as srv:
+        srv.submit("build", 1, big)
+        f = srv.submit("trace", 1, rays)  # waits for the build (same scene)
+        srv.cancel(f)
+        with pytest.raises(CancelledError):
+            f.result(timeout=120)
+        assert srv.cancelled == 1
+        got = srv.submit("trace", 1, rays).result(timeout=120)
+    want = run_plain([(0.0, "build", 1, big), (0.0, "trace", 1, rays)])[1][0]
+    assert hit_mismatches(got, want).size == 0
+
+
+def test_requests_expire_in_the_queue(lib_built):
+    """With max_queue_s, requests that wait longer than that behind other
+    work fail with TimeoutError; the others complete, and an idle server
+    starts new requests at once."""
+    soups = [scenes.soup_large(3_000_000, 96 + k) for k in range(6)]
+    with Server(slots=1, max_queue_s=0.002, batch_max_tris=0) as srv:
+        futs = [srv.submit("build", k, s) for k, s in enumerate(soups)]
+        ok = expired = 0
+        for f in futs:
+            try:
+                f.result(timeout=120)
+                ok += 1
+            except TimeoutError:
+                expired += 1
+        assert expired >= 1 and ok + expired == len(soups)
+        assert srv.expired == expired
+        t = scenes.soup(1_000, 97)
+        srv.submit("build", 100, t).result(timeout=60)
+        assert 100 in srv.resident
