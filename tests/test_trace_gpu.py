@@ -256,7 +256,7 @@ def test_short_stack_settings_match(ctx, port, short_stack):
     assert_hits_equal(got, want)
     assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
     room = scenes.room_scene(seed=21)
-    prim = scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))[::37]
+    prim = np.ascontiguousarray(scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))[::37])
     rnodes = port.build(room, 16)
     want, nb, nt = port.trace(rnodes, room, prim, 16, counts=True)
     got, gb, gt = lb.Traverser(lb.Builder(c)(dev(room)))(prim, counts=True)
