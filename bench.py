@@ -726,8 +726,10 @@ def main():
     ap.add_argument("--step-rays", type=int, default=0,
                     help="profiling: trace only every k-th ray of the headline step (0: all)")
     ap.add_argument("--no-config1", action="store_true", help="skip the mid-size torus step")
-    ap.add_argument("--short-stack", type=int, default=None,
-                    help="traversal stack entries per ray in shared memory (0, 8, 16; default: the library's)")
+    ap.add_argument("--trace-refill", type=int, default=None,
+                    help="idle lanes at which a traversal warp takes new rays (default: the library's)")
+    ap.add_argument("--trace-blocks", type=int, default=None,
+                    help="resident traversal CTAs per SM (default: the library's)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
     ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the served-requests measurement")
@@ -756,10 +758,12 @@ def main():
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     ctx = lb.Context(local, stream.cuda_stream)
-    if args.short_stack is not None:
-        from lbvh_gb300 import _lib
+    from lbvh_gb300 import _lib
 
-        ctx.set_param(_lib.PARAM_TRACE_SHORT_STACK, args.short_stack)
+    if args.trace_refill is not None:
+        ctx.set_param(_lib.PARAM_TRACE_REFILL, args.trace_refill)
+    if args.trace_blocks is not None:
+        ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
 
     def detail(name, rec):
         if rank == 0:

@@ -130,8 +130,6 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             place, each warp's batch of 32 as one 512-byte store (the
                                             traversal then reaches host memory over the CPU-GPU link);
                                             pageable host memory is always copied */
-#define LBVH_PARAM_TRACE_SHORT_STACK 8   /* traversal stack entries per ray kept in shared memory (the
-                                            rest in local memory): 0, 8 or 16 */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

@@ -651,11 +651,6 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "trace in-place mode %d outside [0, 2]", value);
       c->trace_in_place = value;
       return LBVH_OK;
-    case LBVH_PARAM_TRACE_SHORT_STACK:
-      if (value != 0 && value != 8 && value != 16)
-        return fail(c, LBVH_ERR_INVALID_ARG, "short stack %d is not 0, 8 or 16", value);
-      c->trace.short_stack = uint32_t(value);
-      return LBVH_OK;
     case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
       if (value < 1 || value > (1 << 24))
         return fail(c, LBVH_ERR_INVALID_ARG, "look-back spin limit %d outside [1, 2^24]", value);

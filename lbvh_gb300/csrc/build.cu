@@ -53,6 +53,7 @@ template<class Leaf>
 __global__ __launch_bounds__(kBoundsThreads) void
 k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __restrict__ st, Box* __restrict__ box_out)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   __shared__ ArgBox s_part[kBoundsThreads / 32];
   __shared__ bool s_last;
   const uint32_t chunk = ceil_div_u32(n, gridDim.x);
@@ -144,6 +145,7 @@ __global__ __launch_bounds__(kMortonThreads) void
 k_morton(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes, BuildState* __restrict__ st, uint32_t range,
          uint32_t* __restrict__ rows)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   __shared__ uint32_t s_hist[4 * 256];
   __shared__ uint32_t s_top[kTop ? kTopBuckets : 1]; // buckets of the top 12 bits, for the bucket sort
   for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x)
@@ -267,6 +269,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
            uint32_t spin_limit,
            uint32_t wait_xor)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   constexpr int kTile = kSortThreads * kItems;
   if (skip_if_msd && st->use_msd)
     return; // the bucket sort did this build's sorting
@@ -485,6 +488,7 @@ block_excl_scan(uint32_t v, uint32_t* s_warp)
 __global__ __launch_bounds__(1024) void
 k_top_scan(uint32_t* __restrict__ rows, uint32_t nrows, BuildState* __restrict__ st)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   constexpr int kPer = kTopBuckets / 1024;
   constexpr uint32_t kBatch = 8;
   __shared__ uint32_t s_warp[32];
@@ -580,6 +584,7 @@ __global__ __launch_bounds__(kPartThreads) void
 k_partition(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout, uint32_t n, uint32_t range,
             uint32_t group, const uint32_t* __restrict__ rows, const BuildState* __restrict__ st)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   if (!st->use_msd)
     return;
   constexpr int kPer = kTopBuckets / kPartThreads; // buckets per thread in the scans
@@ -673,6 +678,7 @@ k_partition(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout, uint3
 __global__ __launch_bounds__(kBucketThreads, 1) void
 k_bucket_sort(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout, BuildState* __restrict__ st)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   if (!st->use_msd)
     return;
   constexpr int kWarps = kBucketThreads / 32;
@@ -920,6 +926,7 @@ k_tree_local(Leaf leaf,
              uint32_t pending_cap,
              BuildState* __restrict__ st)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   extern __shared__ __align__(32) unsigned char smem[];
   int* s_delta = reinterpret_cast<int*>(smem);                               // kTreeBlock + 1
   uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_delta + kTreeBlock + 8);   // kTreeBlock
@@ -1073,6 +1080,7 @@ k_tree_global(Leaf leaf,
               BuildState* __restrict__ st,
               uint32_t epoch)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= min(__ldg(&st->pending_count), uint32_t(gridDim.x * blockDim.x)))
     return;
@@ -1133,6 +1141,7 @@ k_tree_global_cta(Leaf leaf,
                   uint32_t pending_cap,
                   BuildState* __restrict__ st)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   extern __shared__ uint32_t s_slots[]; // n - 1 split positions
   if (__ldcg(&st->error) & kErrLookbackTimeout)
     return; // the sort gave up: no tree (the error is reported); uniform over the CTA
@@ -1305,6 +1314,7 @@ k_gather_tris(const Tri* __restrict__ tris,
               uint32_t n,
               Tri* __restrict__ out)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
@@ -1318,6 +1328,7 @@ k_gather_boxes(const Box* __restrict__ boxes,
                uint32_t n,
                Box* __restrict__ out)
 {
+  pdl_begin(); // the predecessor in the stream has finished
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n)
     return;
@@ -1328,25 +1339,33 @@ k_gather_boxes(const Box* __restrict__ boxes,
 // ---------------------------------------------------------------------------
 // host-side launchers
 
+#define CUDA_TRY(call)                                                                                                 \
+  do {                                                                                                                 \
+    const cudaError_t e_ = (call);                                                                                     \
+    if (e_ != cudaSuccess)                                                                                             \
+      return e_;                                                                                                       \
+  } while (0)
+
 template<class Leaf>
 static cudaError_t
 launch_curve(const Leaf& leaf, uint32_t n, const BuildBuffers& b, cudaStream_t s, Box* stage)
 {
-  k_bounds<Leaf><<<b.bounds_blocks, kBoundsThreads, 0, s>>>(leaf, n, reinterpret_cast<ArgBox*>(b.partials), b.state,
-                                                            stage);
+  CUDA_TRY(launch_pdl(k_bounds<Leaf>, b.bounds_blocks, kBoundsThreads, 0, s, leaf, n,
+                      reinterpret_cast<ArgBox*>(b.partials), b.state, stage));
   if (stage) {
     if (b.msd)
-      k_morton<BoxLeaf, true><<<b.msd_ranges, kMortonThreads, 0, s>>>(BoxLeaf{ stage }, n, b.keys_a, b.state,
-                                                                      b.msd_range, b.top_rows);
+      CUDA_TRY(launch_pdl(k_morton<BoxLeaf, true>, b.msd_ranges, kMortonThreads, 0, s, BoxLeaf{ stage }, n, b.keys_a,
+                          b.state, b.msd_range, b.top_rows));
     else
-      k_morton<BoxLeaf, false><<<b.morton_blocks, kMortonThreads, 0, s>>>(BoxLeaf{ stage }, n, b.keys_a, b.state, 0,
-                                                                          nullptr);
+      CUDA_TRY(launch_pdl(k_morton<BoxLeaf, false>, b.morton_blocks, kMortonThreads, 0, s, BoxLeaf{ stage }, n,
+                          b.keys_a, b.state, 0, nullptr));
   } else {
     if (b.msd)
-      k_morton<Leaf, true><<<b.msd_ranges, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state, b.msd_range,
-                                                                   b.top_rows);
+      CUDA_TRY(launch_pdl(k_morton<Leaf, true>, b.msd_ranges, kMortonThreads, 0, s, leaf, n, b.keys_a, b.state,
+                          b.msd_range, b.top_rows));
     else
-      k_morton<Leaf, false><<<b.morton_blocks, kMortonThreads, 0, s>>>(leaf, n, b.keys_a, b.state, 0, nullptr);
+      CUDA_TRY(launch_pdl(k_morton<Leaf, false>, b.morton_blocks, kMortonThreads, 0, s, leaf, n, b.keys_a, b.state, 0,
+                          nullptr));
   }
   return cudaGetLastError();
 }
@@ -1371,11 +1390,11 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
       configured.fetch_or(bit, std::memory_order_relaxed);
     }
     // the bucket sort (keys_a -> keys_b -> keys_a), or nothing if a bucket is too large
-    k_top_scan<<<kTopBuckets / 32, 1024, 0, s>>>(b.top_rows, b.msd_ranges, b.state);
+    CUDA_TRY(launch_pdl(k_top_scan, kTopBuckets / 32, 1024, 0, s, b.top_rows, b.msd_ranges, b.state));
     const uint32_t ctas = ceil_div_u32(b.msd_ranges, b.msd_group);
-    k_partition<<<ctas, kPartThreads, kPartSmem, s>>>(b.keys_a, b.keys_b, n, b.msd_range * b.msd_group,
-                                                      b.msd_group, b.top_rows, b.state);
-    k_bucket_sort<<<b.sort_ctas, kBucketThreads, kBucketSmem, s>>>(b.keys_b, b.keys_a, b.state);
+    CUDA_TRY(launch_pdl(k_partition, ctas, kPartThreads, kPartSmem, s, b.keys_a, b.keys_b, n, b.msd_range * b.msd_group,
+                        b.msd_group, b.top_rows, b.state));
+    CUDA_TRY(launch_pdl(k_bucket_sort, b.sort_ctas, kBucketThreads, kBucketSmem, s, b.keys_b, b.keys_a, b.state));
   }
   // the onesweep passes (they return at once when the bucket sort ran);
   // small keys-only sorts use smaller tiles, so that more SMs take part
@@ -1391,18 +1410,17 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
     const uint32_t epoch = epoch_base + pass;
     if (pairs) {
       if (pass == 0)
-        k_onesweep<true, true><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, vb, n, pass, epoch, b.lookback, b.state,
-                                                             false, spin, wx);
+        CUDA_TRY(launch_pdl(k_onesweep<true, true>, tiles, kSortThreads, 0, s, ka, kb, nullptr, vb, n, pass, epoch,
+                            b.lookback, b.state, false, spin, wx));
       else
-        k_onesweep<true, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, va, vb, n, pass, epoch, b.lookback, b.state,
-                                                              false, spin, wx);
+        CUDA_TRY(launch_pdl(k_onesweep<true, false>, tiles, kSortThreads, 0, s, ka, kb, va, vb, n, pass, epoch,
+                            b.lookback, b.state, false, spin, wx));
     } else if (small) {
-      k_onesweep<false, false, kSmallTileItems><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass,
-                                                                              epoch, b.lookback, b.state, msd, spin,
-                                                                              wx);
+      CUDA_TRY(launch_pdl(k_onesweep<false, false, kSmallTileItems>, tiles, kSortThreads, 0, s, ka, kb, nullptr,
+                          nullptr, n, pass, epoch, b.lookback, b.state, msd, spin, wx));
     } else {
-      k_onesweep<false, false><<<tiles, kSortThreads, 0, s>>>(ka, kb, nullptr, nullptr, n, pass, epoch, b.lookback,
-                                                             b.state, msd, spin, wx);
+      CUDA_TRY(launch_pdl(k_onesweep<false, false>, tiles, kSortThreads, 0, s, ka, kb, nullptr, nullptr, n, pass, epoch,
+                          b.lookback, b.state, msd, spin, wx));
     }
     std::swap(ka, kb);
     std::swap(va, vb);
@@ -1433,17 +1451,17 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
   }
   const uint32_t blocks = ceil_div_u32(n, kTreeBlock);
   const uint32_t cap = blocks * kTreePendingPerBlock;
-  k_tree_local<Leaf><<<blocks, kTreeThreads, kTreeSmem, s>>>(leaf, n, b.keys_a, nodes,
-                                                           reinterpret_cast<PendingNode*>(b.pending), cap, b.state);
+  CUDA_TRY(launch_pdl(k_tree_local<Leaf>, blocks, kTreeThreads, kTreeSmem, s, leaf, n, b.keys_a, nodes,
+                      reinterpret_cast<PendingNode*>(b.pending), cap, b.state));
   if (blocks == 1)
     return cudaGetLastError(); // the whole tree was built in the one CTA
   if (n <= kTreeGlobalCtaMaxPrims) {
-    k_tree_global_cta<Leaf><<<1, kTreeGlobalCtaThreads, size_t(4) * (n - 1), s>>>(
-      leaf, n, b.keys_a, nodes, reinterpret_cast<const PendingNode*>(b.pending), cap, b.state);
+    CUDA_TRY(launch_pdl(k_tree_global_cta<Leaf>, 1, kTreeGlobalCtaThreads, size_t(4) * (n - 1), s, leaf, n, b.keys_a,
+                        nodes, reinterpret_cast<const PendingNode*>(b.pending), cap, b.state));
     return cudaGetLastError();
   }
-  k_tree_global<Leaf><<<ceil_div_u32(cap, kFitThreads), kFitThreads, 0, s>>>(
-    leaf, n, b.keys_a, b.slots, nodes, reinterpret_cast<const PendingNode*>(b.pending), b.state, epoch);
+  CUDA_TRY(launch_pdl(k_tree_global<Leaf>, ceil_div_u32(cap, kFitThreads), kFitThreads, 0, s, leaf, n, b.keys_a,
+                      b.slots, nodes, reinterpret_cast<const PendingNode*>(b.pending), b.state, epoch));
   return cudaGetLastError();
 }
 
@@ -1489,14 +1507,14 @@ launch_fit_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, Node* node
 cudaError_t
 launch_gather_tris(const Tri* tris, const uint32_t* perm, uint32_t n, Tri* out, cudaStream_t s)
 {
-  k_gather_tris<<<ceil_div_u32(n, 256), 256, 0, s>>>(tris, perm, n, out);
+  CUDA_TRY(launch_pdl(k_gather_tris, ceil_div_u32(n, 256), 256, 0, s, tris, perm, n, out));
   return cudaGetLastError();
 }
 
 cudaError_t
 launch_gather_boxes(const Box* boxes, const uint32_t* perm, uint32_t n, Box* out, cudaStream_t s)
 {
-  k_gather_boxes<<<ceil_div_u32(n, 256), 256, 0, s>>>(boxes, perm, n, out);
+  CUDA_TRY(launch_pdl(k_gather_boxes, ceil_div_u32(n, 256), 256, 0, s, boxes, perm, n, out));
   return cudaGetLastError();
 }
 

@@ -186,4 +186,40 @@ ceil_div_u32(uint32_t a, uint32_t b)
   return (a + b - 1) / b;
 }
 
+// ---- programmatic dependent launch ----------------------------------------
+//
+// The build's kernels are launched with programmatic stream serialization
+// (launch_pdl): a kernel's CTAs may be scheduled while its predecessor in the
+// stream is still running, so the launch latency between two kernels is
+// hidden. Every such kernel starts with pdl_begin(): wait until the
+// predecessor grid has completed and its writes are visible, then allow the
+// successor to be scheduled. Waiting first means that when a kernel's
+// successor starts, every kernel before this one has finished. Both
+// instructions do nothing for a kernel launched without the attribute.
+__device__ __forceinline__ void
+pdl_begin()
+{
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// kernel<<<grid, block, smem, s>>>(args...) with programmatic stream
+// serialization allowed.
+template<typename... Params, typename... Args>
+inline cudaError_t
+launch_pdl(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args)
+{
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
 } // namespace lbvh_gb300

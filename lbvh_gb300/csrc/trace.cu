@@ -28,11 +28,56 @@ namespace lbvh_gb300 {
 struct RayCtx
 {
   float px, py, pz, dx, dy, dz, tmin, tmax;
-  float rx, ry, rz;   // reciprocal direction
-  float ix, iy, iz;   // (-pos) * rcp
+  float2 rxy, ixy;    // reciprocal direction and (-pos) * rcp, x and y
+  float2 rzz, izz;    // the same for z, twice (paired slab math, see box_pair_fast)
   bool sx, sy, sz;    // dir > 0: near plane is the box minimum
   bool fast;          // no slab value can be NaN: min/max may use fminf/fmaxf
 };
+
+// Packed IEEE single-precision ops on pairs (elementwise, round to nearest,
+// no contraction): each half is exactly what __fmul_rn / __fadd_rn give, so
+// the slab values keep the reference's bits.
+__device__ __forceinline__ float2
+mul2_rn(float2 a, float2 b)
+{
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "mul.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2
+add2_rn(float2 a, float2 b)
+{
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+      "mov.b64 pa, {%2, %3};\n\t"
+      "mov.b64 pb, {%4, %5};\n\t"
+      "add.rn.f32x2 pd, pa, pb;\n\t"
+      "mov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+// Three-input max / min of finite values.
+__device__ __forceinline__ float
+max3f(float a, float b, float c)
+{
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float
+min3f(float a, float b, float c)
+{
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
 
 __device__ __forceinline__ RayCtx
 make_ray(const float4 a, const float4 b)
@@ -47,12 +92,12 @@ make_ray(const float4 a, const float4 b)
   r.tmin = b.z;
   r.tmax = b.w;
   // make_accel_ray, lbvh.h:991-1010
-  r.rx = fdiv(1.0f, r.dx);
-  r.ry = fdiv(1.0f, r.dy);
-  r.rz = fdiv(1.0f, r.dz);
-  r.ix = fmul(-r.px, r.rx);
-  r.iy = fmul(-r.py, r.ry);
-  r.iz = fmul(-r.pz, r.rz);
+  const float rx = fdiv(1.0f, r.dx), ry = fdiv(1.0f, r.dy), rz = fdiv(1.0f, r.dz);
+  const float ix = fmul(-r.px, rx), iy = fmul(-r.py, ry), iz = fmul(-r.pz, rz);
+  r.rxy = make_float2(rx, ry);
+  r.ixy = make_float2(ix, iy);
+  r.rzz = make_float2(rz, rz);
+  r.izz = make_float2(iz, iz);
   r.sx = r.dx > 0.0f;
   r.sy = r.dy > 0.0f;
   r.sz = r.dz > 0.0f;
@@ -66,29 +111,46 @@ make_ray(const float4 a, const float4 b)
 }
 
 // detail::intersect (octant form) + box_intersection::operator bool,
-// lbvh.h:1026-1029, 1071-1091.
+// lbvh.h:1026-1029, 1071-1091, with the reference's NaN-propagating
+// min / max ternaries.
 __device__ __forceinline__ bool
 box_test(const RayCtx& r, float lox, float loy, float loz, float hix, float hiy, float hiz, float& tmin_out)
 {
-  const float tn0 = fadd(fmul(r.sx ? lox : hix, r.rx), r.ix);
-  const float tn1 = fadd(fmul(r.sy ? loy : hiy, r.ry), r.iy);
-  const float tn2 = fadd(fmul(r.sz ? loz : hiz, r.rz), r.iz);
-  const float tf0 = fadd(fmul(r.sx ? hix : lox, r.rx), r.ix);
-  const float tf1 = fadd(fmul(r.sy ? hiy : loy, r.ry), r.iy);
-  const float tf2 = fadd(fmul(r.sz ? hiz : loz, r.rz), r.iz);
-  if (r.fast) {
-    // Finite operands: fmaxf/fminf pick the same value as the reference's
-    // ternaries, up to the sign of a zero, and every later use of tmin/tmax
-    // is a comparison, which ignores that sign.
-    const float tmin = fmaxf(fmaxf(tn0, tn1), tn2);
-    const float tmax = fminf(fminf(tf0, tf1), tf2);
-    tmin_out = tmin;
-    return tmax >= fmaxf(0.0f, tmin);
-  }
+  const float tn0 = fadd(fmul(r.sx ? lox : hix, r.rxy.x), r.ixy.x);
+  const float tn1 = fadd(fmul(r.sy ? loy : hiy, r.rxy.y), r.ixy.y);
+  const float tn2 = fadd(fmul(r.sz ? loz : hiz, r.rzz.x), r.izz.x);
+  const float tf0 = fadd(fmul(r.sx ? hix : lox, r.rxy.x), r.ixy.x);
+  const float tf1 = fadd(fmul(r.sy ? hiy : loy, r.rxy.y), r.ixy.y);
+  const float tf2 = fadd(fmul(r.sz ? hiz : loz, r.rzz.x), r.izz.x);
   const float tmin = mmax(mmax(tn0, tn1), tn2);
   const float tmax = mmin(mmin(tf0, tf1), tf2);
   tmin_out = tmin;
   return tmax >= mmax(0.0f, tmin);
+}
+
+// The same test for both children of a traversal node at once, for a ray
+// and scene whose slab values are all finite (RayCtx::fast): left box
+// lo = (A.x, A.y, A.z), hi = (A.w, B.x, B.y); right box lo = (B.z, B.w, C.x),
+// hi = (C.y, C.z, C.w). Each slab value is b * rcp + inv_pos rounded twice,
+// as in the reference, computed two at a time: the x and y planes of one box
+// as a pair, the z planes of the two boxes as a pair. On finite operands the
+// three-input max / min pick the value the reference's ternaries pick, up to
+// the sign of a zero, and every later use of tmin / tmax is a comparison,
+// which ignores that sign.
+__device__ __forceinline__ void
+box_pair_fast(const RayCtx& r, const float4& A, const float4& B, const float4& C, bool& lhit, bool& rhit, float& lt,
+              float& rt)
+{
+  const float2 ln = add2_rn(mul2_rn(make_float2(r.sx ? A.x : A.w, r.sy ? A.y : B.x), r.rxy), r.ixy);
+  const float2 lf = add2_rn(mul2_rn(make_float2(r.sx ? A.w : A.x, r.sy ? B.x : A.y), r.rxy), r.ixy);
+  const float2 rn = add2_rn(mul2_rn(make_float2(r.sx ? B.z : C.y, r.sy ? B.w : C.z), r.rxy), r.ixy);
+  const float2 rf = add2_rn(mul2_rn(make_float2(r.sx ? C.y : B.z, r.sy ? C.z : B.w), r.rxy), r.ixy);
+  const float2 zn = add2_rn(mul2_rn(make_float2(r.sz ? A.z : B.y, r.sz ? C.x : C.w), r.rzz), r.izz);
+  const float2 zf = add2_rn(mul2_rn(make_float2(r.sz ? B.y : A.z, r.sz ? C.w : C.x), r.rzz), r.izz);
+  lt = max3f(ln.x, ln.y, zn.x);
+  rt = max3f(rn.x, rn.y, zn.y);
+  lhit = min3f(lf.x, lf.y, zf.x) >= fmaxf(0.0f, lt);
+  rhit = min3f(rf.x, rf.y, zf.y) >= fmaxf(0.0f, rt);
 }
 
 // triangle_intersector::operator(), lbvh.h:2055-2075.
@@ -170,12 +232,7 @@ k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict_
 constexpr uint32_t kHitRing = 4;
 constexpr uint32_t kHitDirect = kHitRing; // a ray whose hit is written directly
 
-// kShort > 0: the top kShort entries of each lane's stack live in shared
-// memory (a ring indexed by the logical stack position), the rest in local
-// memory; a push onto a full ring moves the ring's bottom entry to local
-// memory first, a pop from an empty ring reads local memory. The logical
-// stack, its 128-entry capacity and its drop rule are unchanged.
-template<bool kCounts, bool kBatch, bool kHostHits = false, int kShort = 0>
+template<bool kCounts, bool kBatch, bool kHostHits = false>
 __global__ __launch_bounds__(kTraceThreads, 8) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
@@ -203,8 +260,6 @@ k_trace(const WideNode* __restrict__ wnodes,
   // reference's would.
   uint2 stack[kStackSize];
   uint32_t sp = 0;
-  uint32_t lo = 0; // kShort: entries [lo, sp) are in the shared ring, [0, lo) in local memory
-  __shared__ uint2 s_stack[kShort > 0 ? kShort : 1][kTraceThreads];
   uint2 cur = make_uint2(0u, 0u);
   bool has_cur = false;
   uint32_t ray = kMiss; // ray index of this lane, kMiss = none
@@ -325,7 +380,6 @@ k_trace(const WideNode* __restrict__ wnodes,
             nb = tb - lo;
           }
             sp = 0;
-            lo = 0;
             cur = make_uint2(0u, __float_as_uint(inf)); // root, pushed with +inf
             has_cur = true;
             best_p = kMiss;
@@ -346,15 +400,19 @@ k_trace(const WideNode* __restrict__ wnodes,
       const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
       bool lhit = false, rhit = false;
       float lt = inf, rt = inf;
-      if (!(left & kLeafBit)) {
-        if (kCounts)
-          cb++;
-        lhit = box_test(r, A.x, A.y, A.z, A.w, B.x, B.y, lt);
-      }
-      if (!(right & kLeafBit)) {
-        if (kCounts)
-          cb++;
-        rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
+      if (kCounts)
+        cb += uint32_t(!(left & kLeafBit)) + uint32_t(!(right & kLeafBit));
+      if (r.fast) {
+        // both boxes at once; a leaf child's box slot holds zeros, its
+        // result is discarded
+        box_pair_fast(r, A, B, C, lhit, rhit, lt, rt);
+        lhit = lhit && !(left & kLeafBit);
+        rhit = rhit && !(right & kLeafBit);
+      } else {
+        if (!(left & kLeafBit))
+          lhit = box_test(r, A.x, A.y, A.z, A.w, B.x, B.y, lt);
+        if (!(right & kLeafBit))
+          rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
       }
       // leaf triangles, left before right (equal t: the first tested wins)
       if ((left | right) & kLeafBit)
@@ -380,18 +438,8 @@ k_trace(const WideNode* __restrict__ wnodes,
         const bool lfirst = lt < rt; // left nearer: push right, then left
         const uint2 far = lfirst ? make_uint2(right, __float_as_uint(rt)) : make_uint2(left, __float_as_uint(lt));
         const uint2 near = lfirst ? make_uint2(left, __float_as_uint(lt)) : make_uint2(right, __float_as_uint(rt));
-        if (sp < kStackSize) {
-          if (kShort > 0) {
-            if (sp - lo == uint32_t(kShort)) { // ring full: its bottom entry moves to local memory
-              stack[lo] = s_stack[lo % kShort][threadIdx.x];
-              lo++;
-            }
-            s_stack[sp % kShort][threadIdx.x] = far;
-            sp++;
-          } else {
-            stack[sp++] = far;
-          }
-        }
+        if (sp < kStackSize)
+          stack[sp++] = far;
         if (sp < kStackSize) {
           cur = near;
           has_cur = true;
@@ -408,17 +456,7 @@ k_trace(const WideNode* __restrict__ wnodes,
       if (!has_cur) {
         if (sp == 0)
           break;
-        if (kShort > 0) {
-          if (sp == lo) { // the ring is empty: the entry is in local memory
-            cur = stack[--sp];
-            lo = sp;
-          } else {
-            --sp;
-            cur = s_stack[sp % kShort][threadIdx.x];
-          }
-        } else {
-          cur = stack[--sp];
-        }
+        cur = stack[--sp];
       }
       has_cur = !(best_t < __uint_as_float(cur.y));
       if (has_cur)
@@ -484,36 +522,16 @@ launch_trace_tris(const WideNode* wnodes,
   const uint32_t blocks = want < cap ? want : cap;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + n_nodes);
-  auto go = [&](auto kernel, uint32_t* nb, uint32_t* nt) {
-    kernel<<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nb, nt, ray_counter, wide, p.refill,
-                                           nullptr, nullptr, 0);
-  };
-  const bool counts = n_box && n_tri;
-  switch (p.short_stack) {
-    case 8:
-      if (counts)
-        go(k_trace<true, false, false, 8>, n_box, n_tri);
-      else if (host_hits)
-        go(k_trace<false, false, true, 8>, nullptr, nullptr);
-      else
-        go(k_trace<false, false, false, 8>, nullptr, nullptr);
-      break;
-    case 16:
-      if (counts)
-        go(k_trace<true, false, false, 16>, n_box, n_tri);
-      else if (host_hits)
-        go(k_trace<false, false, true, 16>, nullptr, nullptr);
-      else
-        go(k_trace<false, false, false, 16>, nullptr, nullptr);
-      break;
-    default:
-      if (counts)
-        go(k_trace<true, false>, n_box, n_tri);
-      else if (host_hits)
-        go(k_trace<false, false, true>, nullptr, nullptr);
-      else
-        go(k_trace<false, false>, nullptr, nullptr);
-  }
+  if (n_box && n_tri)
+    k_trace<true, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri,
+                                                          ray_counter, wide, p.refill, nullptr, nullptr, 0);
+  else if (host_hits)
+    k_trace<false, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
+                                                                 nullptr, ray_counter, wide, p.refill, nullptr,
+                                                                 nullptr, 0);
+  else
+    k_trace<false, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
+                                                           ray_counter, wide, p.refill, nullptr, nullptr, 0);
   return cudaGetLastError();
 }
 

@@ -13,7 +13,6 @@ struct TraceParams
 {
   uint32_t blocks_per_sm = 8; // resident 128-thread blocks per SM
   uint32_t refill = 12;       // idle lanes at which a warp takes new rays
-  uint32_t short_stack = 0;   // stack entries per lane kept in shared memory: 0, 8 or 16
 };
 
 // Traversal copy of an internal node: both children's boxes plus the child

@@ -232,35 +232,3 @@ def test_pinned_traces_in_place_match_device_traces(ctx, mode):
         assert lb.hits_view(hits_p[1:].view(m, 4)).tobytes() == ref, mode
     finally:
         ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, 2)
-
-
-@pytest.mark.parametrize("short_stack", [0, 8, 16])
-def test_short_stack_settings_match(ctx, port, short_stack):
-    """Every setting of the shared-memory short stack gives the reference's
-    hits and per-ray test counts: the golden fixtures (duplicate-code and
-    all-equal inputs build deep trees, whose stacks overflow the ring into
-    local memory), the small config in full, a slice of the large room."""
-    from lbvh_gb300 import _lib
-
-    c = lb.Context()
-    c.set_param(_lib.PARAM_TRACE_SHORT_STACK, short_stack)
-    for name in [n for n in GOLDEN if n != "soup2000_boxes"]:
-        g = load_golden(name)
-        got = lb.hits_view(lb.Traverser(lb.Builder(c)(dev(g["tris"])))(dev(g["rays"])))
-        assert_hits_equal(got, g["hits"])
-    t = scenes.soup(968, seed=1)
-    rays = scenes.pinhole_rays(256, 256)
-    nodes = port.build(t, 8)
-    want, nb, nt = port.trace(nodes, t, rays, 16, counts=True)
-    got, gb, gt = lb.Traverser(lb.Builder(c)(dev(t)))(rays, counts=True)
-    assert_hits_equal(got, want)
-    assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
-    room = scenes.room_scene(seed=21)
-    prim = np.ascontiguousarray(scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))[::37])
-    rnodes = port.build(room, 16)
-    want, nb, nt = port.trace(rnodes, room, prim, 16, counts=True)
-    got, gb, gt = lb.Traverser(lb.Builder(c)(dev(room)))(prim, counts=True)
-    assert_hits_equal(got, want)
-    assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
-    with pytest.raises(ValueError):
-        c.set_param(_lib.PARAM_TRACE_SHORT_STACK, 4)
