@@ -34,22 +34,12 @@ struct RayCtx
   bool fast;          // no slab value can be NaN: min/max may use fminf/fmaxf
 };
 
-// Packed IEEE single-precision ops on pairs (elementwise, round to nearest,
-// no contraction): each half is exactly what __fmul_rn / __fadd_rn give, so
-// the slab values keep the reference's bits.
-__device__ __forceinline__ float2
-mul2_rn(float2 a, float2 b)
-{
-  float2 d;
-  asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
-      "mov.b64 pa, {%2, %3};\n\t"
-      "mov.b64 pb, {%4, %5};\n\t"
-      "mul.rn.f32x2 pd, pa, pb;\n\t"
-      "mov.b64 {%0, %1}, pd;\n\t}"
-      : "=f"(d.x), "=f"(d.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-  return d;
-}
+// Packed IEEE single-precision add on a pair (elementwise, round to
+// nearest): each half is exactly what __fadd_rn gives. Only the add is
+// packed. The products feeding it are scalar __fmul_rn: the assembler may
+// contract a packed multiply that feeds a packed add into one fused
+// multiply-add (measured on sm_103a, despite .rn), which would round
+// b * rcp + inv_pos once instead of twice and change grazing hits.
 __device__ __forceinline__ float2
 add2_rn(float2 a, float2 b)
 {
@@ -132,21 +122,27 @@ box_test(const RayCtx& r, float lox, float loy, float loz, float hix, float hiy,
 // and scene whose slab values are all finite (RayCtx::fast): left box
 // lo = (A.x, A.y, A.z), hi = (A.w, B.x, B.y); right box lo = (B.z, B.w, C.x),
 // hi = (C.y, C.z, C.w). Each slab value is b * rcp + inv_pos rounded twice,
-// as in the reference, computed two at a time: the x and y planes of one box
-// as a pair, the z planes of the two boxes as a pair. On finite operands the
+// as in the reference, the adds two at a time: the x and y planes of one
+// box as a pair, the z planes of the two boxes as a pair. On finite operands the
 // three-input max / min pick the value the reference's ternaries pick, up to
 // the sign of a zero, and every later use of tmin / tmax is a comparison,
 // which ignores that sign.
+__device__ __forceinline__ float2
+mul_pair(float a, float b, float2 m)
+{
+  return make_float2(fmul(a, m.x), fmul(b, m.y));
+}
+
 __device__ __forceinline__ void
 box_pair_fast(const RayCtx& r, const float4& A, const float4& B, const float4& C, bool& lhit, bool& rhit, float& lt,
               float& rt)
 {
-  const float2 ln = add2_rn(mul2_rn(make_float2(r.sx ? A.x : A.w, r.sy ? A.y : B.x), r.rxy), r.ixy);
-  const float2 lf = add2_rn(mul2_rn(make_float2(r.sx ? A.w : A.x, r.sy ? B.x : A.y), r.rxy), r.ixy);
-  const float2 rn = add2_rn(mul2_rn(make_float2(r.sx ? B.z : C.y, r.sy ? B.w : C.z), r.rxy), r.ixy);
-  const float2 rf = add2_rn(mul2_rn(make_float2(r.sx ? C.y : B.z, r.sy ? C.z : B.w), r.rxy), r.ixy);
-  const float2 zn = add2_rn(mul2_rn(make_float2(r.sz ? A.z : B.y, r.sz ? C.x : C.w), r.rzz), r.izz);
-  const float2 zf = add2_rn(mul2_rn(make_float2(r.sz ? B.y : A.z, r.sz ? C.w : C.x), r.rzz), r.izz);
+  const float2 ln = add2_rn(mul_pair(r.sx ? A.x : A.w, r.sy ? A.y : B.x, r.rxy), r.ixy);
+  const float2 lf = add2_rn(mul_pair(r.sx ? A.w : A.x, r.sy ? B.x : A.y, r.rxy), r.ixy);
+  const float2 rn = add2_rn(mul_pair(r.sx ? B.z : C.y, r.sy ? B.w : C.z, r.rxy), r.ixy);
+  const float2 rf = add2_rn(mul_pair(r.sx ? C.y : B.z, r.sy ? C.z : B.w, r.rxy), r.ixy);
+  const float2 zn = add2_rn(mul_pair(r.sz ? A.z : B.y, r.sz ? C.x : C.w, r.rzz), r.izz);
+  const float2 zf = add2_rn(mul_pair(r.sz ? B.y : A.z, r.sz ? C.w : C.x, r.rzz), r.izz);
   lt = max3f(ln.x, ln.y, zn.x);
   rt = max3f(rn.x, rn.y, zn.y);
   lhit = min3f(lf.x, lf.y, zf.x) >= fmaxf(0.0f, lt);
