@@ -730,6 +730,8 @@ def main():
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
                     help="resident traversal CTAs per SM (default: the library's)")
+    ap.add_argument("--trace-leaf-batch", type=int, default=None,
+                    help="lanes with pending triangle tests before a traversal warp runs them (default: the library's)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
     ap.add_argument("--only-batched", action="store_true", help="only the batched-meshes measurement")
     ap.add_argument("--no-served", action="store_true", help="skip the served-requests measurement")
@@ -764,6 +766,8 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_REFILL, args.trace_refill)
     if args.trace_blocks is not None:
         ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
+    if args.trace_leaf_batch is not None:
+        ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
 
     def detail(name, rec):
         if rank == 0:

@@ -130,6 +130,9 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             place, each warp's batch of 32 as one 512-byte store (the
                                             traversal then reaches host memory over the CPU-GPU link);
                                             pageable host memory is always copied */
+#define LBVH_PARAM_TRACE_LEAF_BATCH 8    /* lanes of a traversal warp with pending leaf-triangle tests
+                                            before the warp runs them together, 1..32 (1: each lane tests
+                                            its triangles right after its visit); results do not change */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

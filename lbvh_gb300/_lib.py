@@ -34,6 +34,7 @@ PARAM_TRACE_CHUNK = 4
 PARAM_TRACE_IN_PLACE = 5
 PARAM_LOOKBACK_SPIN_LIMIT = 6
 PARAM_TEST_LOOKBACK_STALL = 7
+PARAM_TRACE_LEAF_BATCH = 8
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000

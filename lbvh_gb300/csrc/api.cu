@@ -651,6 +651,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "trace in-place mode %d outside [0, 2]", value);
       c->trace_in_place = value;
       return LBVH_OK;
+    case LBVH_PARAM_TRACE_LEAF_BATCH:
+      if (value < 1 || value > 32)
+        return fail(c, LBVH_ERR_INVALID_ARG, "leaf batch %d outside [1, 32]", value);
+      c->trace.leaf_batch = uint32_t(value);
+      return LBVH_OK;
     case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
       if (value < 1 || value > (1 << 24))
         return fail(c, LBVH_ERR_INVALID_ARG, "look-back spin limit %d outside [1, 2^24]", value);

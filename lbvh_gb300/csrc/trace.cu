@@ -228,8 +228,12 @@ k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict_
 constexpr uint32_t kHitRing = 4;
 constexpr uint32_t kHitDirect = kHitRing; // a ray whose hit is written directly
 
+#ifndef LBVH_TRACE_MIN_BLOCKS
+#define LBVH_TRACE_MIN_BLOCKS 8 // resident CTAs per SM the register budget is set for
+#endif
+
 template<bool kCounts, bool kBatch, bool kHostHits = false>
-__global__ __launch_bounds__(kTraceThreads, 8) void
+__global__ __launch_bounds__(kTraceThreads, LBVH_TRACE_MIN_BLOCKS) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
         const uint32_t* __restrict__ leaf_prim,
@@ -241,6 +245,7 @@ k_trace(const WideNode* __restrict__ wnodes,
         uint32_t* __restrict__ ray_counter,
         const uint32_t* __restrict__ wide,
         uint32_t refill,
+        uint32_t leaf_batch,
         const uint32_t* __restrict__ moff,
         const uint32_t* __restrict__ roff,
         uint32_t n_meshes)
@@ -258,6 +263,8 @@ k_trace(const WideNode* __restrict__ wnodes,
   uint32_t sp = 0;
   uint2 cur = make_uint2(0u, 0u);
   bool has_cur = false;
+  bool pend = false;                   // the leaf children of the last visit are not yet tested
+  uint32_t leaf_l = kMiss, leaf_r = kMiss; // those leaf children (kMiss: an internal child)
   uint32_t ray = kMiss; // ray index of this lane, kMiss = none
   RayCtx r{};
   uint32_t best_p = kMiss;
@@ -386,11 +393,11 @@ k_trace(const WideNode* __restrict__ wnodes,
         }
       }
     }
-    if (ray == kMiss)
-      continue;
+    const bool busy = ray != kMiss;
 
-    // ---- one node visit (lbvh.h:1902-1938); cur passed the cull test ----
-    {
+    // ---- one node visit (lbvh.h:1902-1938) for the lanes whose previous
+    // visit is complete; cur passed the cull test ----
+    if (busy && !pend) {
       const float4* w = reinterpret_cast<const float4*>(wnodes + nb + cur.x);
       const float4 A = __ldg(w + 0), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
       const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
@@ -410,24 +417,11 @@ k_trace(const WideNode* __restrict__ wnodes,
         if (!(right & kLeafBit))
           rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
       }
-      // leaf triangles, left before right (equal t: the first tested wins)
-      if ((left | right) & kLeafBit)
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        const uint32_t c = k == 0 ? left : right;
-        if (c & kLeafBit) {
-          const uint32_t p = c & ~kLeafBit;
-          float t, u, v;
-          if (kCounts)
-            ct++;
-          if (tri_test(r, tris + tb, p, t, u, v) && t < best_t) {
-            best_p = p;
-            best_t = t;
-            best_u = u;
-            best_v = v;
-          }
-        }
-      }
+      // leaf children: tested below, left before right, before this lane's
+      // next pop (so its cull test sees their hits, as in the reference)
+      leaf_l = (left & kLeafBit) ? (left & ~kLeafBit) : kMiss;
+      leaf_r = (right & kLeafBit) ? (right & ~kLeafBit) : kMiss;
+      pend = ((left | right) & kLeafBit) != 0;
       // pushes; the last one pushed stays in registers as the next pop
       has_cur = false;
       if (lhit && rhit) {
@@ -447,6 +441,36 @@ k_trace(const WideNode* __restrict__ wnodes,
         }
       }
     }
+
+    // ---- leaf triangles of the pending lanes (equal t: the first tested
+    // wins). The block costs the warp the same whether one lane or many run
+    // it, so a lane with pending triangles sits out node visits until
+    // leaf_batch lanes are pending, or until no lane is left to visit; each
+    // ray still visits, tests and pops in the reference's order. ----
+    const uint32_t pmask = __ballot_sync(0xffffffffu, pend);
+    if (pmask && (uint32_t(__popc(pmask)) >= leaf_batch || __ballot_sync(0xffffffffu, busy && !pend) == 0)) {
+      if (pend) {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          const uint32_t p = k == 0 ? leaf_l : leaf_r;
+          if (p != kMiss) {
+            float t, u, v;
+            if (kCounts)
+              ct++;
+            if (tri_test(r, tris + tb, p, t, u, v) && t < best_t) {
+              best_p = p;
+              best_t = t;
+              best_u = u;
+              best_v = v;
+            }
+          }
+        }
+        pend = false;
+      }
+    }
+    if (!busy || pend)
+      continue;
+
     // ---- next entry: pop until one passes the cull test (lbvh.h:1893-1900) ----
     for (;;) {
       if (!has_cur) {
@@ -520,14 +544,14 @@ launch_trace_tris(const WideNode* wnodes,
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + n_nodes);
   if (n_box && n_tri)
     k_trace<true, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri,
-                                                          ray_counter, wide, p.refill, nullptr, nullptr, 0);
+                                                          ray_counter, wide, p.refill, p.leaf_batch, nullptr, nullptr, 0);
   else if (host_hits)
     k_trace<false, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
-                                                                 nullptr, ray_counter, wide, p.refill, nullptr,
-                                                                 nullptr, 0);
+                                                                 nullptr, ray_counter, wide, p.refill, p.leaf_batch,
+                                                                 nullptr, nullptr, 0);
   else
     k_trace<false, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
-                                                           ray_counter, wide, p.refill, nullptr, nullptr, 0);
+                                                           ray_counter, wide, p.refill, p.leaf_batch, nullptr, nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -753,8 +777,8 @@ launch_batch_trace(const WideNode* wnodes,
   const uint32_t blocks = want < cap ? want : cap;
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + total_nodes);
   k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, reinterpret_cast<const float4*>(rays),
-                                                        m, hits, nullptr, nullptr, ray_counter, wide, p.refill, off,
-                                                        roff, n_meshes);
+                                                        m, hits, nullptr, nullptr, ray_counter, wide, p.refill,
+                                                        p.leaf_batch, off, roff, n_meshes);
   return cudaGetLastError();
 }
 

@@ -232,3 +232,34 @@ def test_pinned_traces_in_place_match_device_traces(ctx, mode):
         assert lb.hits_view(hits_p[1:].view(m, 4)).tobytes() == ref, mode
     finally:
         ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, 2)
+
+
+@pytest.mark.parametrize("leaf_batch", [1, 4, 32])
+def test_leaf_batch_settings_match(ctx, port, leaf_batch):
+    """Every setting of the traversal's leaf batching gives the reference's
+    hits and per-ray box / triangle test counts (each ray keeps the
+    reference's visit, test and cull order): the golden fixtures, the small
+    config in full, and a slice of the large room's primary rays."""
+    from lbvh_gb300 import _lib
+
+    c = lb.Context()
+    c.set_param(_lib.PARAM_TRACE_LEAF_BATCH, leaf_batch)
+    for name in [n for n in GOLDEN if n != "soup2000_boxes"]:
+        g = load_golden(name)
+        got = lb.hits_view(lb.Traverser(lb.Builder(c)(dev(g["tris"])))(dev(g["rays"])))
+        assert_hits_equal(got, g["hits"])
+    t = scenes.soup(968, seed=1)
+    rays = scenes.pinhole_rays(256, 256)
+    nodes = port.build(t, 8)
+    want, nb, nt = port.trace(nodes, t, rays, 16, counts=True)
+    got, gb, gt = lb.Traverser(lb.Builder(c)(dev(t)))(rays, counts=True)
+    assert_hits_equal(got, want)
+    assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
+    room = scenes.room_scene(seed=21)
+    prim = np.ascontiguousarray(scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))[::37])
+    want, nb, nt = port.trace(port.build(room, 16), room, prim, 16, counts=True)
+    got, gb, gt = lb.Traverser(lb.Builder(c)(dev(room)))(prim, counts=True)
+    assert_hits_equal(got, want)
+    assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
+    with pytest.raises(ValueError):
+        c.set_param(_lib.PARAM_TRACE_LEAF_BATCH, 0)
