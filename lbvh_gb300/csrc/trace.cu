@@ -25,21 +25,9 @@
 
 namespace lbvh_gb300 {
 
-// A ray as the triangle and sphere tests use it (lbvh.h:388-401).
-struct RayGeom
-{
-  float px, py, pz, dx, dy, dz, tmin, tmax;
-};
-
-__device__ __forceinline__ RayGeom
-ray_geom(const float4 a, const float4 b)
-{
-  return RayGeom{ a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w };
-}
-
-// A ray as the box test uses it (make_accel_ray, lbvh.h:991-1010).
 struct RayCtx
 {
+  float px, py, pz, dx, dy, dz, tmin, tmax;
   float2 rxy, ixy;    // reciprocal direction and (-pos) * rcp, x and y
   float2 rzz, izz;    // the same for z, twice (paired slab math, see box_pair_fast)
   bool sx, sy, sz;    // dir > 0: near plane is the box minimum
@@ -85,23 +73,30 @@ __device__ __forceinline__ RayCtx
 make_ray(const float4 a, const float4 b)
 {
   RayCtx r;
-  const RayGeom g = ray_geom(a, b);
+  r.px = a.x;
+  r.py = a.y;
+  r.pz = a.z;
+  r.dx = a.w;
+  r.dy = b.x;
+  r.dz = b.y;
+  r.tmin = b.z;
+  r.tmax = b.w;
   // make_accel_ray, lbvh.h:991-1010
-  const float rx = fdiv(1.0f, g.dx), ry = fdiv(1.0f, g.dy), rz = fdiv(1.0f, g.dz);
-  const float ix = fmul(-g.px, rx), iy = fmul(-g.py, ry), iz = fmul(-g.pz, rz);
+  const float rx = fdiv(1.0f, r.dx), ry = fdiv(1.0f, r.dy), rz = fdiv(1.0f, r.dz);
+  const float ix = fmul(-r.px, rx), iy = fmul(-r.py, ry), iz = fmul(-r.pz, rz);
   r.rxy = make_float2(rx, ry);
   r.ixy = make_float2(ix, iy);
   r.rzz = make_float2(rz, rz);
   r.izz = make_float2(iz, iz);
-  r.sx = g.dx > 0.0f;
-  r.sy = g.dy > 0.0f;
-  r.sz = g.dz > 0.0f;
+  r.sx = r.dx > 0.0f;
+  r.sy = r.dy > 0.0f;
+  r.sz = r.dz > 0.0f;
   // |dir| >= 2^-60 and |pos| <= 2^60 (false for NaN), with every box
   // coordinate within 2^60 (checked by k_repack), bound |b * rcp| and
   // |pos * rcp| by 2^120: every slab value is finite.
   const float lo = 0x1p-60f, hi = 0x1p60f;
-  r.fast = fabsf(g.dx) >= lo && fabsf(g.dy) >= lo && fabsf(g.dz) >= lo && fabsf(g.px) <= hi &&
-           fabsf(g.py) <= hi && fabsf(g.pz) <= hi;
+  r.fast = fabsf(r.dx) >= lo && fabsf(r.dy) >= lo && fabsf(r.dz) >= lo && fabsf(r.px) <= hi &&
+           fabsf(r.py) <= hi && fabsf(r.pz) <= hi;
   return r;
 }
 
@@ -156,7 +151,7 @@ box_pair_fast(const RayCtx& r, const float4& A, const float4& B, const float4& C
 
 // triangle_intersector::operator(), lbvh.h:2055-2075.
 __device__ __forceinline__ bool
-tri_test(const RayGeom& r, const Tri* __restrict__ tris, uint32_t p, float& t, float& u, float& v)
+tri_test(const RayCtx& r, const Tri* __restrict__ tris, uint32_t p, float& t, float& u, float& v)
 {
   const float4* q = reinterpret_cast<const float4*>(tris + p);
   const float4 A = __ldg(q + 0), B = __ldg(q + 1), C = __ldg(q + 2);
@@ -272,13 +267,9 @@ k_trace(const WideNode* __restrict__ wnodes,
   uint32_t leaf_l = kMiss, leaf_r = kMiss; // those leaf children (kMiss: an internal child)
   uint32_t ray = kMiss; // ray index of this lane, kMiss = none
   RayCtx r{};
-  uint32_t best_p = kMiss; // the closest hit so far (its u, v are recomputed at the end)
-  float best_t = inf;
+  uint32_t best_p = kMiss;
+  float best_t = inf, best_u = 0.0f, best_v = 0.0f;
   uint32_t cb = 0, ct = 0;
-  // Each lane's ray as loaded, for the triangle tests: kept in shared memory
-  // rather than in 8 registers (the box tests use only RayCtx), so that more
-  // warps fit on an SM.
-  __shared__ float4 s_ray[2][kTraceThreads];
   uint32_t nb = 0, tb = 0; // batched: the ray's mesh node and triangle bases
 
   // the warp's current batch of 32 ray ids (warp-uniform state)
@@ -377,10 +368,7 @@ k_trace(const WideNode* __restrict__ wnodes,
             ray = id;
             if (kHostHits)
               buf = id_buf;
-            const float4 ra = __ldg(rays + 2 * size_t(id)), rb = __ldg(rays + 2 * size_t(id) + 1);
-            s_ray[0][threadIdx.x] = ra; // read back only by this thread
-            s_ray[1][threadIdx.x] = rb;
-            r = make_ray(ra, rb);
+            r = make_ray(__ldg(rays + 2 * size_t(id)), __ldg(rays + 2 * size_t(id) + 1));
             r.fast = r.fast && scene_fast;
           if (kBatch) { // the mesh k with roff[k] <= id < roff[k + 1]
             uint32_t lo = 0, hi = n_meshes; // invariant: roff[lo] <= id < roff[hi]
@@ -399,6 +387,7 @@ k_trace(const WideNode* __restrict__ wnodes,
             has_cur = true;
             best_p = kMiss;
             best_t = inf;
+            best_u = best_v = 0.0f;
             cb = ct = 0;
           }
         }
@@ -461,7 +450,6 @@ k_trace(const WideNode* __restrict__ wnodes,
     const uint32_t pmask = __ballot_sync(0xffffffffu, pend);
     if (pmask && (uint32_t(__popc(pmask)) >= leaf_batch || __ballot_sync(0xffffffffu, busy && !pend) == 0)) {
       if (pend) {
-        const RayGeom g = ray_geom(s_ray[0][threadIdx.x], s_ray[1][threadIdx.x]);
 #pragma unroll
         for (int k = 0; k < 2; k++) {
           const uint32_t p = k == 0 ? leaf_l : leaf_r;
@@ -469,9 +457,11 @@ k_trace(const WideNode* __restrict__ wnodes,
             float t, u, v;
             if (kCounts)
               ct++;
-            if (tri_test(g, tris + tb, p, t, u, v) && t < best_t) {
+            if (tri_test(r, tris + tb, p, t, u, v) && t < best_t) {
               best_p = p;
               best_t = t;
+              best_u = u;
+              best_v = v;
             }
           }
         }
@@ -496,11 +486,8 @@ k_trace(const WideNode* __restrict__ wnodes,
       Hit h;
       h.prim = (best_p != kMiss && leaf_prim) ? __ldg(leaf_prim + tb + best_p) : best_p;
       h.t = best_t;
-      h.u = h.v = 0.0f;
-      if (best_p != kMiss) { // the winner's u, v: the same test gives the same bits
-        float t;
-        tri_test(ray_geom(s_ray[0][threadIdx.x], s_ray[1][threadIdx.x]), tris + tb, best_p, t, h.u, h.v);
-      }
+      h.u = best_p != kMiss ? best_u : 0.0f;
+      h.v = best_p != kMiss ? best_v : 0.0f;
       if (kHostHits && buf != kHitDirect) {
         s_hits[wid][buf][ray - s_first[wid][buf]] = h;
         flush = atomicSub(&s_left[wid][buf], 1u) == 1u; // the batch's last ray
@@ -587,7 +574,7 @@ struct SphereInfo
 // from atan2 / acos. A ray that misses returns t = +inf. The ray's tmin and
 // tmax are not consulted, as in the example.
 __device__ __forceinline__ SphereInfo
-sphere_test(const RayGeom& r, float4 s)
+sphere_test(const RayCtx& r, float4 s)
 {
   const float inf = __int_as_float(0x7f800000);
   const float rad = s.x, cx = s.y, cy = s.z, cz = s.w;
@@ -622,9 +609,7 @@ k_trace_spheres(const WideNode* __restrict__ wnodes,
   const float inf = __int_as_float(0x7f800000);
   uint2 stack[kStackSize];
   for (uint32_t ray = blockIdx.x * blockDim.x + threadIdx.x; ray < m; ray += gridDim.x * blockDim.x) {
-    const float4 ra = __ldg(rays + 2 * size_t(ray)), rb = __ldg(rays + 2 * size_t(ray) + 1);
-    const RayGeom g = ray_geom(ra, rb);
-    RayCtx r = make_ray(ra, rb);
+    RayCtx r = make_ray(__ldg(rays + 2 * size_t(ray)), __ldg(rays + 2 * size_t(ray) + 1));
     r.fast = false; // the reference's own min/max ternaries throughout
     uint32_t best_p = kMiss;
     SphereInfo best{ inf, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f };
@@ -641,7 +626,7 @@ k_trace_spheres(const WideNode* __restrict__ wnodes,
       float lt = inf, rt = inf;
       if (left & kLeafBit) {
         const uint32_t p = left & ~kLeafBit;
-        const SphereInfo h = sphere_test(g, __ldg(spheres + p));
+        const SphereInfo h = sphere_test(r, __ldg(spheres + p));
         if (h.t < best.t) {
           best = h;
           best_p = p;
@@ -651,7 +636,7 @@ k_trace_spheres(const WideNode* __restrict__ wnodes,
       }
       if (right & kLeafBit) {
         const uint32_t p = right & ~kLeafBit;
-        const SphereInfo h = sphere_test(g, __ldg(spheres + p));
+        const SphereInfo h = sphere_test(r, __ldg(spheres + p));
         if (h.t < best.t) {
           best = h;
           best_p = p;
