@@ -272,6 +272,8 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
     import lbvh_gb300 as lb
     from lbvh_gb300 import scenes
 
+    from lbvh_gb300 import autotune
+
     host = scenes.soup_large(n, seed=16)
     if span != 1.0:
         host[0] = -span
@@ -279,6 +281,7 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
     soup = torch.from_numpy(host).to(dev)
     big = lb.BVH(ctx)
     ctx.reserve(n, 0)
+    tuning = autotune.tune_build(ctx, soup)  # this size class's sort / bounds setting
     for _ in range(3):
         builder(soup, into=big)
     torch.cuda.synchronize()
@@ -314,6 +317,7 @@ def measure_build_16m(ctx, builder, stream, flush, dev, steps, hbm_peak, peak_ki
     return {"triangles": n, "ms": round(ms16, 4),
             "mprims_s": round(n / (ms16 * 1e-3) / 1e6, 1),
             "refit_ms": refit_ms,
+            "tuning": tuning,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "bytes_per_prim": sum(BYTES_PER_PRIM.values()),
@@ -531,7 +535,8 @@ def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_
            "workload": f"batch{n_meshes}_loguniform64-65536_{rays_per_mesh}rays"}
     with torch.cuda.stream(s):
         setting = autotune.tune_batch(ctx, tris, off, rays, roff, key=f"gb300:{res['workload']}")
-        res["tuning"] = {k: setting[k] for k in ("batch_threads", "trace_blocks_per_sm", "trace_refill")}
+        res["tuning"] = {k: setting[k] for k in ("batch_threads", "batch_radix_bits", "batch_keys_per_thread",
+                                                 "trace_blocks_per_sm", "trace_refill", "trace_leaf_batch")}
         batch = lb.Batch(ctx)
         for _ in range(3):
             batch.build(tris, off)
@@ -674,6 +679,9 @@ def measure_config1(ctx, stream, flush, dev, steps):
     tris = torch.from_numpy(tris_h).to(dev)
     rays = torch.from_numpy(rays_h).to(dev)
     hits = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=dev)
+    from lbvh_gb300 import autotune
+
+    tuning = autotune.tune_build(ctx, tris)  # this size class's sort / bounds setting
     builder, bvh = lb.Builder(ctx), lb.BVH(ctx)
     builder(tris, into=bvh)
     trav = lb.Traverser(bvh)
@@ -685,7 +693,8 @@ def measure_config1(ctx, stream, flush, dev, steps):
     m = rays.shape[0]
     return {"workload": CONFIG1_WORKLOAD, "triangles": int(tris_h.shape[0]), "rays_per_step": int(m),
             "value": round(m / ((b + tr) * 1e-3) / 1e6, 1), "unit": "Mrays/s", "ms_per_step": round(b + tr, 4),
-            "build_ms": round(b, 4), "trace_ms": round(tr, 4)}
+            "build_ms": round(b, 4), "trace_ms": round(tr, 4),
+            "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")}}
 
 
 def summary_line(line):
@@ -696,6 +705,8 @@ def summary_line(line):
     if b16:
         out["build_16m"] = {"ms": b16["ms"], "mprims_s": b16["mprims_s"], "refit_ms": b16["refit_ms"],
                             "frac": b16["roofline"]["frac"]}
+        t16 = b16.get("tuning") or {}
+        out["build_16m"]["tuning"] = [t16.get(k) for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")]
     c1 = line.get("config1")
     if c1:
         out["config1"] = {k: c1[k] for k in ("value", "ms_per_step", "build_ms", "trace_ms")}
@@ -703,7 +714,9 @@ def summary_line(line):
     if bt:
         out["batched"] = {"graph_step_ms": bt.get("graph_step_ms"), "plain_step_ms": bt["plain_step_ms"],
                           "speedup_vs_plain": bt["speedup_vs_plain"],
-                          "sorted_leaves_step_ms": bt["sorted_leaves"]["step_ms"]}
+                          "sorted_leaves_step_ms": bt["sorted_leaves"]["step_ms"],
+                          "tuning": [bt["tuning"].get(k) for k in ("batch_threads", "batch_radix_bits",
+                                                                     "batch_keys_per_thread")]}
     sv = line.get("served")
     if sv:
         out["served"] = {k: {"ratio": v["throughput_ratio"], "p99_ms": [v["server"]["p99_ms"], v["plain"]["p99_ms"]],
@@ -796,6 +809,9 @@ def main():
     builder = lb.Builder(ctx)
     bvh = lb.BVH(ctx)
     ctx.reserve(n, prim.shape[0])
+    from lbvh_gb300 import autotune
+
+    tuning = autotune.tune_build(ctx, tris)  # the room's size class: sort / bounds setting
     builder(tris, into=bvh)
     trav = lb.Traverser(bvh)
     trav(prim, out=hits_p)
@@ -874,10 +890,12 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": config,
-        "build": {"ms": round(build_ms, 4), "mprims_s": round(n / (build_ms * 1e-3) / 1e6, 1)},
+        "build": {"ms": round(build_ms, 4), "mprims_s": round(n / (build_ms * 1e-3) / 1e6, 1),
+                  "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")}},
         "trace": {"ms": round(trace_ms, 4), "mrays_s": round(m / (trace_ms * 1e-3) / 1e6, 1),
                   "primary_hit_fraction": round(hit_frac, 4)},
     }
+    detail("build_tuning", tuning)
     if args.only_step:
         line["gpu_launches"] = gpu_launches
         line["clocks"] = clk

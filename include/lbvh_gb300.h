@@ -133,6 +133,14 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_TRACE_LEAF_BATCH 8    /* lanes of a traversal warp with pending leaf-triangle tests
                                             before the warp runs them together, 1..32 (1: each lane tests
                                             its triangles right after its visit); results do not change */
+#define LBVH_PARAM_BATCH_RADIX_BITS 9     /* digit width of the batched build's CTA-local radix sort: 4, 6
+                                            or 8 bits (8, 5 or 4 passes over the 30-bit codes) */
+#define LBVH_PARAM_BATCH_KEYS_PER_THREAD 10 /* keys per thread in each chunk that sort ranks: 4 or 8 */
+#define LBVH_PARAM_SORT_TILE_KEYS 11     /* keys per tile of a keys-only onesweep sort: 0 (default: 1,024 up
+                                            to 65,536 codes, else 4,096), 1024 or 4096 */
+#define LBVH_PARAM_BUCKET_SORT_MIN 12    /* keys-only builds of at least this many primitives sort by
+                                            buckets of the top 12 code bits (>= 65,536; default 1,500,000) */
+#define LBVH_PARAM_BOUNDS_BLOCKS_PER_SM 13 /* CTAs per SM of the bounds pass, 1..16 (default 4) */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

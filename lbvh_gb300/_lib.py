@@ -35,6 +35,11 @@ PARAM_TRACE_IN_PLACE = 5
 PARAM_LOOKBACK_SPIN_LIMIT = 6
 PARAM_TEST_LOOKBACK_STALL = 7
 PARAM_TRACE_LEAF_BATCH = 8
+PARAM_BATCH_RADIX_BITS = 9
+PARAM_BATCH_KEYS_PER_THREAD = 10
+PARAM_SORT_TILE_KEYS = 11
+PARAM_BUCKET_SORT_MIN = 12
+PARAM_BOUNDS_BLOCKS_PER_SM = 13
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000

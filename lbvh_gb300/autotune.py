@@ -1,10 +1,20 @@
-"""Autotuner for the GPU launch shapes (results are unaffected; only speed).
+"""Autotuner for the GPU launch shapes and sort parameters (results are
+unaffected; only speed).
 
 Tunes, on a caller-supplied sample workload:
-  * the CTA size of the batched build (LBVH_PARAM_BATCH_THREADS: 256, 512,
-    1024 threads; each sort chunk is CTA size x 4 keys, 8-bit radix digits);
-  * the persistent traversal grid (LBVH_PARAM_TRACE_BLOCKS_PER_SM) and the
-    ray-refill threshold (LBVH_PARAM_TRACE_REFILL).
+  * the batched build (tune_batch): its CTA size (LBVH_PARAM_BATCH_THREADS:
+    256, 512, 1024 threads), the radix width of its CTA-local sort
+    (LBVH_PARAM_BATCH_RADIX_BITS: 4, 6 or 8-bit digits, i.e. 8, 5 or 4 passes)
+    and the keys each thread ranks per chunk (LBVH_PARAM_BATCH_KEYS_PER_THREAD:
+    4 or 8); then the persistent traversal grid
+    (LBVH_PARAM_TRACE_BLOCKS_PER_SM), the ray-refill threshold
+    (LBVH_PARAM_TRACE_REFILL) and the leaf-test batching
+    (LBVH_PARAM_TRACE_LEAF_BATCH) of the batched trace;
+  * the plain build (tune_build), per size class (primitive counts in
+    [2^k, 2^(k+1))): the keys-only sort's tile (LBVH_PARAM_SORT_TILE_KEYS:
+    1,024 or 4,096 keys), whether the bucket sort runs
+    (LBVH_PARAM_BUCKET_SORT_MIN) and the bounds pass's CTAs per SM
+    (LBVH_PARAM_BOUNDS_BLOCKS_PER_SM).
 The best setting per workload key is kept in a JSON table (by default
 $LBVH_TUNE_CACHE, else ~/.cache/lbvh_gb300/tuning.json) and applied to a
 context with apply().
@@ -19,8 +29,37 @@ import numpy as np
 from . import _lib
 
 BATCH_THREADS = (256, 512, 1024)
+BATCH_RADIX_BITS = (4, 6, 8)
+BATCH_KEYS_PER_THREAD = (4, 8)
 TRACE_BLOCKS_PER_SM = (6, 8)
 TRACE_REFILL = (8, 12, 16)
+TRACE_LEAF_BATCH = (1, 8)
+SORT_TILE_KEYS = (1024, 4096)
+BOUNDS_BLOCKS_PER_SM = (2, 4, 8)
+BUCKET_SORT_MIN = 65536  # the smallest size the bucket sort may take
+BUCKET_SORT_OFF = 1 << 30  # a threshold no build reaches
+
+# setting key -> context parameter
+_PARAMS = {
+    "batch_threads": "PARAM_BATCH_THREADS",
+    "batch_radix_bits": "PARAM_BATCH_RADIX_BITS",
+    "batch_keys_per_thread": "PARAM_BATCH_KEYS_PER_THREAD",
+    "trace_blocks_per_sm": "PARAM_TRACE_BLOCKS_PER_SM",
+    "trace_refill": "PARAM_TRACE_REFILL",
+    "trace_leaf_batch": "PARAM_TRACE_LEAF_BATCH",
+    "sort_tile_keys": "PARAM_SORT_TILE_KEYS",
+    "bucket_sort_min": "PARAM_BUCKET_SORT_MIN",
+    "bounds_blocks_per_sm": "PARAM_BOUNDS_BLOCKS_PER_SM",
+}
+
+
+def size_class(n: int) -> int:
+    """The size class of a build of n primitives: k with 2^k <= n < 2^(k+1)."""
+    return max(int(n), 1).bit_length() - 1
+
+
+def build_key(n: int, device: str = "gb300") -> str:
+    return f"{device}:build:2^{size_class(n)}"
 
 
 def cache_path() -> str:
@@ -50,12 +89,19 @@ def save_table(table: dict, path: str | None = None) -> None:
 
 
 def apply(ctx, setting: dict) -> None:
-    if "batch_threads" in setting:
-        ctx.set_param(_lib.PARAM_BATCH_THREADS, int(setting["batch_threads"]))
-    if "trace_blocks_per_sm" in setting:
-        ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, int(setting["trace_blocks_per_sm"]))
-    if "trace_refill" in setting:
-        ctx.set_param(_lib.PARAM_TRACE_REFILL, int(setting["trace_refill"]))
+    """Sets the context parameters a setting names (other keys -- the
+    timings kept beside them -- are ignored)."""
+    for key, name in _PARAMS.items():
+        if key in setting:
+            ctx.set_param(getattr(_lib, name), int(setting[key]))
+
+
+def apply_build(ctx, n: int, table_path: str | None = None, device: str = "gb300") -> dict | None:
+    """Applies the tuned plain-build setting of n's size class, if any."""
+    setting = load_table(table_path).get(build_key(n, device))
+    if setting:
+        apply(ctx, setting)
+    return setting
 
 
 def _time(fn, stream, reps: int) -> float:
@@ -75,10 +121,19 @@ def _time(fn, stream, reps: int) -> float:
     return float(np.median(ts))
 
 
+def _store(table, key, setting, table_path):
+    table[key] = setting
+    try:
+        save_table(table, table_path)
+    except OSError:
+        pass  # a read-only home: keep the setting for this process only
+
+
 def tune_batch(ctx, tris, offsets, rays, ray_offsets, key: str, reps: int = 3, table_path: str | None = None,
                force: bool = False) -> dict:
-    """Best launch shapes for a batched build + trace workload (device
-    arrays); cached under `key`. Returns the setting and applies it."""
+    """Best build and trace parameters for a batched build + trace workload
+    (device arrays); cached under `key`. Returns the setting and applies
+    it."""
     import torch
 
     from .api import Batch
@@ -92,25 +147,66 @@ def tune_batch(ctx, tris, offsets, rays, ray_offsets, key: str, reps: int = 3, t
     out = torch.empty((rays.shape[0], 4), dtype=torch.float32, device=rays.device)
     build_ms = {}
     for t in BATCH_THREADS:
-        ctx.set_param(_lib.PARAM_BATCH_THREADS, t)
-        build_ms[t] = _time(lambda: batch.build(tris, offsets), stream, reps)
-    best_t = min(build_ms, key=build_ms.get)
-    ctx.set_param(_lib.PARAM_BATCH_THREADS, best_t)
+        for bits in BATCH_RADIX_BITS:
+            for items in BATCH_KEYS_PER_THREAD:
+                apply(ctx, {"batch_threads": t, "batch_radix_bits": bits, "batch_keys_per_thread": items})
+                build_ms[(t, bits, items)] = _time(lambda: batch.build(tris, offsets), stream, reps)
+    best_t, best_bits, best_items = min(build_ms, key=build_ms.get)
+    apply(ctx, {"batch_threads": best_t, "batch_radix_bits": best_bits, "batch_keys_per_thread": best_items})
     batch.build(tris, offsets)
     trace_ms = {}
     for bps in TRACE_BLOCKS_PER_SM:
         for refill in TRACE_REFILL:
-            ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, bps)
-            ctx.set_param(_lib.PARAM_TRACE_REFILL, refill)
-            trace_ms[(bps, refill)] = _time(lambda: batch.trace(rays, ray_offsets, out=out), stream, reps)
-    bps, refill = min(trace_ms, key=trace_ms.get)
-    setting = {"batch_threads": best_t, "trace_blocks_per_sm": bps, "trace_refill": refill,
-               "build_ms": {str(k): round(v, 4) for k, v in build_ms.items()},
-               "trace_ms": {f"{k[0]}x{k[1]}": round(v, 4) for k, v in trace_ms.items()}}
-    table[key] = setting
-    try:
-        save_table(table, table_path)
-    except OSError:
-        pass  # a read-only home: keep the setting for this process only
+            for leaf in TRACE_LEAF_BATCH:
+                apply(ctx, {"trace_blocks_per_sm": bps, "trace_refill": refill, "trace_leaf_batch": leaf})
+                trace_ms[(bps, refill, leaf)] = _time(lambda: batch.trace(rays, ray_offsets, out=out), stream, reps)
+    bps, refill, leaf = min(trace_ms, key=trace_ms.get)
+    setting = {"batch_threads": best_t, "batch_radix_bits": best_bits, "batch_keys_per_thread": best_items,
+               "trace_blocks_per_sm": bps, "trace_refill": refill, "trace_leaf_batch": leaf,
+               "build_ms": {"x".join(map(str, k)): round(v, 4) for k, v in build_ms.items()},
+               "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in trace_ms.items()}}
+    _store(table, key, setting, table_path)
     apply(ctx, setting)
     return setting
+
+
+def build_candidates(n: int) -> list[dict]:
+    """The plain-build settings tried for a build of n primitives."""
+    out = []
+    for tile in SORT_TILE_KEYS:
+        for bounds in BOUNDS_BLOCKS_PER_SM:
+            out.append({"sort_tile_keys": tile, "bucket_sort_min": BUCKET_SORT_OFF, "bounds_blocks_per_sm": bounds})
+    if n >= BUCKET_SORT_MIN:
+        for bounds in BOUNDS_BLOCKS_PER_SM:
+            out.append({"sort_tile_keys": 0, "bucket_sort_min": BUCKET_SORT_MIN, "bounds_blocks_per_sm": bounds})
+    return out
+
+
+def tune_build(ctx, tris, reps: int = 5, table_path: str | None = None, force: bool = False,
+               device: str = "gb300") -> dict:
+    """Best plain-build setting for the size class of `tris` (a device
+    triangle array), timed on that array; cached per size class. Returns
+    the setting and applies it."""
+    import torch
+
+    from .api import BVH, Builder
+
+    n = int(tris.shape[0])
+    key = build_key(n, device)
+    table = load_table(table_path)
+    if key in table and not force:
+        apply(ctx, table[key])
+        return table[key]
+    stream = torch.cuda.current_stream()
+    builder, bvh = Builder(ctx), BVH(ctx)
+    ms = []
+    for cand in build_candidates(n):
+        apply(ctx, cand)
+        ms.append(_time(lambda: builder(tris, into=bvh), stream, reps))
+    best = dict(build_candidates(n)[int(np.argmin(ms))])
+    best["build_ms"] = {f"tile{c['sort_tile_keys']}_bucket{int(c['bucket_sort_min'] < BUCKET_SORT_OFF)}"
+                        f"_bounds{c['bounds_blocks_per_sm']}": round(t, 4) for c, t in zip(build_candidates(n), ms)}
+    best["tuned_on"] = n
+    _store(table, key, best, table_path)
+    apply(ctx, best)
+    return best

@@ -58,6 +58,11 @@ struct lbvh_ctx
   int trace_in_place = 2;               // LBVH_PARAM_TRACE_IN_PLACE
   TraceParams trace;               // traversal launch shape
   uint32_t batch_threads = 512;    // CTA size of the batched build
+  uint32_t batch_radix_bits = 8;   // digit width of the batched build's CTA-local sort
+  uint32_t batch_items = 4;        // keys per thread of its ranked chunks
+  uint32_t tile_keys = 0;          // keys-only sort tile (0: by size)
+  uint32_t msd_min = kMsdMinPrims; // keys-only builds from this size use the bucket sort
+  uint32_t bounds_per_sm = 4;      // bounds-pass CTAs per SM
   DevBuf batch_ws;                 // batched build: codes, boxes, slots
   uint32_t epoch = 0;          // look-back epoch of the last sort pass
   char msg[512] = { 0 };
@@ -180,7 +185,7 @@ uint32_t
 bounds_blocks_for(const lbvh_ctx* c, uint32_t n)
 {
   const uint32_t want = ceil_div_u32(n, kBoundsThreads);
-  const uint32_t cap = uint32_t(c->num_sms) * 4;
+  const uint32_t cap = uint32_t(c->num_sms) * c->bounds_per_sm;
   return want < 1 ? 1 : (want > cap ? cap : want);
 }
 
@@ -196,7 +201,7 @@ morton_blocks_for(const lbvh_ctx* c, uint32_t n)
 int
 ws_reserve(lbvh_ctx* c, size_t n)
 {
-  const size_t tiles = sort_tiles(n);
+  const size_t tiles = sort_tiles_any(n);
   const size_t A = 256;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -204,7 +209,7 @@ ws_reserve(lbvh_ctx* c, size_t n)
     off = align_up(off + bytes, A);
     return o;
   };
-  const size_t o_part = take(size_t(c->num_sms) * 4 * 48);
+  const size_t o_part = take(size_t(c->num_sms) * kMaxBoundsBlocksPerSm * 48);
   const size_t o_ka = take(4 * n);
   const size_t o_kb = take(4 * n);
   const size_t o_va = take(4 * n);
@@ -333,7 +338,8 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
   b.morton_blocks = morton_blocks_for(c, nn);
   const bool keep = flags & LBVH_BUILD_KEEP_CURVE;
   const bool sorted_leaves = flags & LBVH_BUILD_SORTED_LEAVES;
-  b.msd = !keep && !sorted_leaves && nn >= kMsdMinPrims; // keys-only sort of a large build
+  b.msd = !keep && !sorted_leaves && nn >= c->msd_min; // keys-only sort of a large build
+  b.tile_keys = c->tile_keys;
   if (b.msd) {
     // ranges of at least one partition tile, a few per SM; their count rows
     // (ranges x 16 KB <= 2n + 16 KB) live in vals_a, unused by keys-only sorts
@@ -655,6 +661,31 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
       if (value < 1 || value > 32)
         return fail(c, LBVH_ERR_INVALID_ARG, "leaf batch %d outside [1, 32]", value);
       c->trace.leaf_batch = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_BATCH_RADIX_BITS:
+      if (value != 4 && value != 6 && value != 8)
+        return fail(c, LBVH_ERR_INVALID_ARG, "batch radix width %d is not 4, 6 or 8 bits", value);
+      c->batch_radix_bits = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_BATCH_KEYS_PER_THREAD:
+      if (value != 4 && value != 8)
+        return fail(c, LBVH_ERR_INVALID_ARG, "batch keys per thread %d is not 4 or 8", value);
+      c->batch_items = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_SORT_TILE_KEYS:
+      if (value != 0 && value != kSmallTile && value != kSortTile)
+        return fail(c, LBVH_ERR_INVALID_ARG, "sort tile %d is not 0, %d or %d keys", value, kSmallTile, kSortTile);
+      c->tile_keys = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_BUCKET_SORT_MIN:
+      if (value < 65536)
+        return fail(c, LBVH_ERR_INVALID_ARG, "bucket-sort threshold %d below 65536", value);
+      c->msd_min = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_BOUNDS_BLOCKS_PER_SM:
+      if (value < 1 || value > int(kMaxBoundsBlocksPerSm))
+        return fail(c, LBVH_ERR_INVALID_ARG, "bounds CTAs per SM %d outside [1, %u]", value, kMaxBoundsBlocksPerSm);
+      c->bounds_per_sm = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
       if (value < 1 || value > (1 << 24))
@@ -1259,7 +1290,7 @@ lbvh_batch_build(lbvh_ctx* c, const float* tris, size_t total, const uint32_t* o
     bb.sorted_tris = static_cast<Tri*>(b->sorted_tris.ptr);
   }
   CK(launch_batch_build(static_cast<const Tri*>(dt), bb, static_cast<Node*>(b->nodes.ptr), c->batch_threads,
-                        c->num_sms, c->stream),
+                        c->batch_radix_bits, c->batch_items, c->num_sms, c->stream),
      "batch build launch");
   b->n_meshes = uint32_t(n_meshes);
   b->total = uint32_t(total);

@@ -94,15 +94,20 @@ scan256(uint32_t v, uint32_t* s_tmp)
   return r;
 }
 
-// One CTA per mesh at a time (see the file comment). Dynamic shared memory:
-// one 256-counter histogram per warp for the chunk ranking.
-template<bool kSorted>
+// One CTA per mesh at a time (see the file comment). The sort uses digits of
+// kBits bits (ceil(30 / kBits) passes over the 30-bit codes) and ranks
+// chunks of kItems keys per thread. Dynamic shared memory: one
+// 2^kBits-counter histogram per warp for the chunk ranking.
+template<bool kSorted, int kBits, int kItems>
 __global__ __launch_bounds__(kBatchMaxThreads) void
 k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ nodes)
 {
-  extern __shared__ uint32_t s_whist[]; // [warps][256]
-  __shared__ uint32_t s_hist[4][256];
-  __shared__ uint32_t s_run[256];
+  constexpr uint32_t kDigits = 1u << kBits;
+  constexpr uint32_t kPasses = (30 + kBits - 1) / kBits;
+  static_assert(kDigits <= 256, "the digit scan covers 256 counters");
+  extern __shared__ uint32_t s_whist[]; // [warps][kDigits]
+  __shared__ uint32_t s_hist[kPasses][kDigits];
+  __shared__ uint32_t s_run[kDigits];
   __shared__ ArgBox s_part[32];
   __shared__ uint32_t s_tmp[32];
   __shared__ float s_lo[3], s_scale[3];
@@ -151,7 +156,7 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
       }
     }
     a = block_reduce_arg(a, s_part);
-    for (uint32_t k = tid; k < 4 * 256; k += nthreads)
+    for (uint32_t k = tid; k < kPasses * kDigits; k += nthreads)
       (&s_hist[0][0])[k] = 0;
     if (tid == 0) {
 #pragma unroll
@@ -174,73 +179,72 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
         const uint32_t z = __float2uint_rz(fmul(fsub(fmul(fadd(bx.lo[2], bx.hi[2]), 0.5f), lo2), sc2));
         const uint32_t code = (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
         b.keys_a[s0 + i] = code;
-        atomicAdd(&s_hist[0][code & 255u], 1u);
-        atomicAdd(&s_hist[1][(code >> 8) & 255u], 1u);
-        atomicAdd(&s_hist[2][(code >> 16) & 255u], 1u);
-        atomicAdd(&s_hist[3][code >> 24], 1u);
+#pragma unroll
+        for (uint32_t pass = 0; pass < kPasses; pass++)
+          atomicAdd(&s_hist[pass][(code >> (pass * kBits)) & (kDigits - 1)], 1u);
       }
     }
     __syncthreads();
 
-    // ---- 3. stable LSD radix sort of the mesh's codes, 4 x 8 bits ----
+    // ---- 3. stable LSD radix sort of the mesh's codes, kPasses x kBits bits ----
     uint32_t* src = b.keys_a + s0;
     uint32_t* dst = b.keys_b + s0;
     uint32_t* vsrc = kSorted ? b.vals_a + s0 : nullptr; // pass 0 generates the indices
     uint32_t* vdst = kSorted ? b.vals_b + s0 : nullptr;
-    const uint32_t chunk = nthreads * kBatchItems;
-    for (uint32_t pass = 0; pass < 4; pass++) {
-      const uint32_t shift = pass * 8;
-      const uint32_t start = scan256(tid < 256 ? s_hist[pass][tid] : 0u, s_tmp);
-      if (tid < 256)
+    const uint32_t chunk = nthreads * kItems;
+    for (uint32_t pass = 0; pass < kPasses; pass++) {
+      const uint32_t shift = pass * kBits;
+      const uint32_t start = scan256(tid < kDigits ? s_hist[pass][tid] : 0u, s_tmp);
+      if (tid < kDigits)
         s_run[tid] = start;
       for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
-        for (uint32_t k = tid; k < nwarps * 256; k += nthreads)
+        for (uint32_t k = tid; k < nwarps * kDigits; k += nthreads)
           s_whist[k] = 0;
         __syncthreads();
-        uint32_t key[kBatchItems], dig[kBatchItems], rank[kBatchItems], val[kSorted ? kBatchItems : 1];
+        uint32_t key[kItems], dig[kItems], rank[kItems], val[kSorted ? kItems : 1];
 #pragma unroll
-        for (int k = 0; k < kBatchItems; k++) {
-          const uint32_t idx = c0 + warp * (32 * kBatchItems) + uint32_t(k) * 32 + lane;
+        for (int k = 0; k < kItems; k++) {
+          const uint32_t idx = c0 + warp * (32 * kItems) + uint32_t(k) * 32 + lane;
           key[k] = idx < n ? __ldcg(src + idx) : 0u;
-          dig[k] = idx < n ? (key[k] >> shift) & 255u : 256u;
+          dig[k] = idx < n ? (key[k] >> shift) & (kDigits - 1) : kDigits; // kDigits: not a key
           if (kSorted)
             val[kSorted ? k : 0] = idx < n ? (pass == 0 ? idx : __ldcg(vsrc + idx)) : 0u;
         }
         // warp ranking: items in (k, lane) order are in index order
 #pragma unroll
-        for (int k = 0; k < kBatchItems; k++) {
+        for (int k = 0; k < kItems; k++) {
           const uint32_t d = dig[k];
           const uint32_t peers = __match_any_sync(0xffffffffu, d);
           const uint32_t pre = __popc(peers & lt_mask);
           uint32_t before = 0;
-          if (d < 256)
-            before = s_whist[warp * 256 + d];
+          if (d < kDigits)
+            before = s_whist[warp * kDigits + d];
           __syncwarp();
-          if (d < 256 && pre == 0)
-            s_whist[warp * 256 + d] = before + __popc(peers);
+          if (d < kDigits && pre == 0)
+            s_whist[warp * kDigits + d] = before + __popc(peers);
           __syncwarp();
           rank[k] = before + pre;
         }
         __syncthreads();
         uint32_t total = 0;
-        if (tid < 256) {
+        if (tid < kDigits) {
           for (uint32_t w = 0; w < nwarps; w++) {
-            const uint32_t c = s_whist[w * 256 + tid];
-            s_whist[w * 256 + tid] = total;
+            const uint32_t c = s_whist[w * kDigits + tid];
+            s_whist[w * kDigits + tid] = total;
             total += c;
           }
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < kBatchItems; k++)
-          if (dig[k] < 256) {
-            const uint32_t at = s_run[dig[k]] + s_whist[warp * 256 + dig[k]] + rank[k];
+        for (int k = 0; k < kItems; k++)
+          if (dig[k] < kDigits) {
+            const uint32_t at = s_run[dig[k]] + s_whist[warp * kDigits + dig[k]] + rank[k];
             dst[at] = key[k];
             if (kSorted)
               vdst[at] = val[kSorted ? k : 0];
           }
         __syncthreads();
-        if (tid < 256)
+        if (tid < kDigits)
           s_run[tid] += total;
       }
       __syncthreads();
@@ -253,7 +257,15 @@ k_batch_build(const Tri* __restrict__ tris, BatchBuffers b, Node* __restrict__ n
         vdst = t;
       }
     }
-    // four passes: the sorted codes are back in keys_a (the permutation in vals_a)
+    if (kPasses % 2) { // an odd pass count ends in keys_b / vals_b: move the result back
+      for (uint32_t i = tid; i < n; i += nthreads) {
+        b.keys_a[s0 + i] = __ldcg(b.keys_b + s0 + i);
+        if (kSorted)
+          b.vals_a[s0 + i] = __ldcg(b.vals_b + s0 + i);
+      }
+      __syncthreads();
+    }
+    // the sorted codes are in keys_a (the permutation in vals_a)
     if (kSorted) { // each mesh's triangles in leaf order, for the trace
       const uint32_t* perm = b.vals_a + s0;
       const float4* in = reinterpret_cast<const float4*>(tris + s0);
@@ -355,22 +367,50 @@ k_batch_gate(const uint32_t* __restrict__ error, uint32_t* __restrict__ queue, u
   *queue = (*error & kErrBadTopology) ? n_meshes : 0u;
 }
 
+template<bool kSorted, int kBits>
+static cudaError_t
+launch_batch_kernel(uint32_t items, uint32_t grid, uint32_t threads, const Tri* tris, const BatchBuffers& b, Node* nodes,
+                    cudaStream_t s)
+{
+  const size_t smem = size_t(threads / 32) * (1u << kBits) * 4;
+  if (items == 8)
+    k_batch_build<kSorted, kBits, 8><<<grid, threads, smem, s>>>(tris, b, nodes);
+  else
+    k_batch_build<kSorted, kBits, 4><<<grid, threads, smem, s>>>(tris, b, nodes);
+  return cudaGetLastError();
+}
+
+template<bool kSorted>
+static cudaError_t
+launch_batch_sorted(uint32_t radix_bits, uint32_t items, uint32_t grid, uint32_t threads, const Tri* tris,
+                    const BatchBuffers& b, Node* nodes, cudaStream_t s)
+{
+  switch (radix_bits) {
+    case 4:
+      return launch_batch_kernel<kSorted, 4>(items, grid, threads, tris, b, nodes, s);
+    case 6:
+      return launch_batch_kernel<kSorted, 6>(items, grid, threads, tris, b, nodes, s);
+    default:
+      return launch_batch_kernel<kSorted, 8>(items, grid, threads, tris, b, nodes, s);
+  }
+}
+
 cudaError_t
-launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t threads, int num_sms, cudaStream_t s)
+launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t threads, uint32_t radix_bits,
+                   uint32_t items, int num_sms, cudaStream_t s)
 {
   if (threads < 256 || threads > kBatchMaxThreads || threads % 32)
+    return cudaErrorInvalidValue;
+  if ((radix_bits != 4 && radix_bits != 6 && radix_bits != 8) || (items != 4 && items != 8))
     return cudaErrorInvalidValue;
   k_check_offsets<<<ceil_div_u32(b.n_meshes, 256), 256, 0, s>>>(b.off, b.n_meshes, b.total, b.error);
   k_batch_gate<<<1, 1, 0, s>>>(b.error, b.queue, b.n_meshes);
   const uint32_t per_sm = 2048 / threads;
   const uint32_t cap = uint32_t(num_sms) * per_sm;
   const uint32_t grid = b.n_meshes < cap ? b.n_meshes : cap;
-  const size_t smem = size_t(threads / 32) * 256 * 4;
   if (b.sorted_tris)
-    k_batch_build<true><<<grid, threads, smem, s>>>(tris, b, nodes);
-  else
-    k_batch_build<false><<<grid, threads, smem, s>>>(tris, b, nodes);
-  return cudaGetLastError();
+    return launch_batch_sorted<true>(radix_bits, items, grid, threads, tris, b, nodes, s);
+  return launch_batch_sorted<false>(radix_bits, items, grid, threads, tris, b, nodes, s);
 }
 
 } // namespace lbvh_gb300

@@ -6,7 +6,6 @@
 
 namespace lbvh_gb300 {
 
-constexpr int kBatchItems = 4;         // keys per thread per sort chunk
 constexpr int kBatchMaxThreads = 1024; // largest CTA of the batched build
 
 // Device views for one batched build of n_meshes meshes, total triangles.
@@ -34,8 +33,11 @@ struct BatchBuffers
 // the mesh in stable Morton order (the plain build's sorted-leaf mode, mesh by
 // mesh): the permutation ends in b.vals_a, the reordered triangles in
 // b.sorted_tris.
-cudaError_t launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t threads, int num_sms,
-                               cudaStream_t s);
+// threads: CTA size (256..1024, a multiple of 32); radix_bits: digit width
+// of the CTA-local sort (4, 6 or 8 bits: 8, 5 or 4 passes over the 30-bit
+// codes); items: keys per thread in each ranked chunk (4 or 8).
+cudaError_t launch_batch_build(const Tri* tris, const BatchBuffers& b, Node* nodes, uint32_t threads,
+                               uint32_t radix_bits, uint32_t items, int num_sms, cudaStream_t s);
 
 // Traversal copy of every mesh's nodes (local child references), plus the
 // scene-bound flag word after the last node.

@@ -1398,7 +1398,7 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
   }
   // the onesweep passes (they return at once when the bucket sort ran);
   // small keys-only sorts use smaller tiles, so that more SMs take part
-  const bool small = !pairs && n <= kSmallTileMaxPrims;
+  const bool small = !pairs && (b.tile_keys ? b.tile_keys == uint32_t(kSmallTile) : n <= kSmallTileMaxPrims);
   const uint32_t tiles = ceil_div_u32(n, small ? kSmallTile : kSortTile);
   uint32_t* ka = b.keys_a;
   uint32_t* kb = b.keys_b;

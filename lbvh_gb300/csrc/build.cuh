@@ -22,6 +22,12 @@ constexpr size_t sort_tiles(size_t n)
 {
   return n <= kSmallTileMaxPrims ? (n + kSmallTile - 1) / kSmallTile : (n + kSortTile - 1) / kSortTile;
 }
+// look-back words for any tile choice (the smaller tiles need the most)
+constexpr size_t sort_tiles_any(size_t n)
+{
+  return (n + kSmallTile - 1) / kSmallTile;
+}
+constexpr uint32_t kMaxBoundsBlocksPerSm = 16; // bounds-pass CTAs per SM a context may ask for
 // Keys-only sort of large builds: partition by the top 12 code bits, then
 // sort each bucket by its low 18 bits in shared memory (used when every
 // bucket fits).
@@ -100,6 +106,8 @@ struct BuildBuffers
   uint32_t msd_group;             // bucket sort: ranges per CTA of the partition
   uint32_t sort_ctas;             // bucket sort: persistent CTAs (one per SM)
   uint32_t* top_rows;             // bucket sort: msd_ranges x kTopBuckets counts (in vals_a)
+  uint32_t tile_keys;             // keys-only onesweep tile: 0 automatic (kSmallTile up to
+                                  // kSmallTileMaxPrims codes, else kSortTile), or kSmallTile / kSortTile
   uint32_t spin_limit;            // look-back polls before a wait gives up (0: kSpinLimit)
   uint32_t wait_xor;              // test only: nonzero makes every look-back wait for a tag no
                                   // tile publishes, so each wait runs out (0 in normal use)

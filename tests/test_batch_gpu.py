@@ -47,6 +47,34 @@ def test_batch_build_matches_oracle(ctx, port, threads):
         ctx.set_param(_lib.PARAM_BATCH_THREADS, 512)
 
 
+@pytest.mark.parametrize("bits,items", [(4, 4), (6, 4), (6, 8), (8, 8), (4, 8)])
+@pytest.mark.parametrize("sorted_leaves", [False, True])
+def test_batch_radix_width_and_keys_per_thread(ctx, port, bits, items, sorted_leaves):
+    """Every radix width (4, 6, 8 bits: an even and an odd number of passes)
+    and keys-per-thread setting of the CTA-local sort gives every mesh the
+    plain build's node block (and, with sorted leaves, its leaf order)."""
+    ctx.set_param(_lib.PARAM_BATCH_RADIX_BITS, bits)
+    ctx.set_param(_lib.PARAM_BATCH_KEYS_PER_THREAD, items)
+    try:
+        meshes, tris, off = make_batch([2, 3, 64, 1000, 4097, 20000, 65536], bits * 10 + items)
+        b = lb.Batch(ctx).build(dev(tris), off, sorted_leaves=sorted_leaves)
+        all_nodes = b.nodes()
+        for k, m in enumerate(meshes):
+            if sorted_leaves:
+                perm = port.curve(m, 8)[2]
+                want = port.build(m[perm], 8)
+            else:
+                want = port.build(m, 8)
+            assert nodes_equal(b.mesh_nodes(k, all_nodes), want), (bits, items, k, m.shape[0])
+    finally:
+        ctx.set_param(_lib.PARAM_BATCH_RADIX_BITS, 8)
+        ctx.set_param(_lib.PARAM_BATCH_KEYS_PER_THREAD, 4)
+    with pytest.raises(ValueError):
+        ctx.set_param(_lib.PARAM_BATCH_RADIX_BITS, 5)
+    with pytest.raises(ValueError):
+        ctx.set_param(_lib.PARAM_BATCH_KEYS_PER_THREAD, 6)
+
+
 def test_batch_trace_matches_oracle(ctx, port):
     meshes, tris, off = make_batch([2, 17, 500, 3000, 40000], 7)
     b = lb.Batch(ctx).build(dev(tris), off)

@@ -179,6 +179,31 @@ def test_lookback_wait_that_runs_out_reports_timeout(lib_built, port, sorted_lea
         assert nodes_equal(got.nodes(), port.build(t, 16))
 
 
+@pytest.mark.parametrize("tile,bucket_min,bounds", [(1024, 1 << 30, 2), (4096, 1 << 30, 8), (0, 65536, 1),
+                                                     (0, 65536, 16), (1024, 1 << 30, 16)])
+def test_sort_and_bounds_parameters(lib_built, port, tile, bucket_min, bounds):
+    """The plain build's tunable sort and bounds parameters (tile size of
+    the keys-only sort, the bucket sort for builds from 65,536 primitives,
+    the bounds pass's CTAs per SM) all give the reference's nodes: random
+    soups around the tile and bucket boundaries, the clustered room and a
+    duplicate-heavy input."""
+    from lbvh_gb300 import _lib
+
+    c = lb.Context()
+    c.set_param(_lib.PARAM_SORT_TILE_KEYS, tile)
+    c.set_param(_lib.PARAM_BUCKET_SORT_MIN, bucket_min)
+    c.set_param(_lib.PARAM_BOUNDS_BLOCKS_PER_SM, bounds)
+    cases = [scenes.soup(n, 90 + n % 7) for n in (2, 1000, 4097, 65536, 65537, 300_007)]
+    cases.append(scenes.room_scene(seed=21))
+    cases.append(load_golden("dups4000")["tris"])
+    for t in cases:
+        assert nodes_equal(lb.Builder(c)(dev(t)).nodes(), port.build(t, 16)), (tile, bucket_min, bounds, t.shape[0])
+    for param, bad in ((_lib.PARAM_SORT_TILE_KEYS, 2048), (_lib.PARAM_BUCKET_SORT_MIN, 1000),
+                       (_lib.PARAM_BOUNDS_BLOCKS_PER_SM, 17)):
+        with pytest.raises(ValueError):
+            c.set_param(param, bad)
+
+
 def test_full_size_16m_build_parity(ctx, port):
     """The 16M-triangle random soup (the roofline workload) against the
     oracle, bit for bit, plus the reference's structural invariants."""
