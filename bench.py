@@ -684,6 +684,7 @@ def measure_config1(ctx, stream, flush, dev, steps):
     tuning = autotune.tune_build(ctx, tris)  # this size class's sort / bounds setting
     builder, bvh = lb.Builder(ctx), lb.BVH(ctx)
     builder(tris, into=bvh)
+    trace_tuning = autotune.tune_trace(ctx, bvh, rays, key=f"gb300:trace:{CONFIG1_WORKLOAD}")
     trav = lb.Traverser(bvh)
     for _ in range(3):
         builder(tris, into=bvh)
@@ -694,7 +695,8 @@ def measure_config1(ctx, stream, flush, dev, steps):
     return {"workload": CONFIG1_WORKLOAD, "triangles": int(tris_h.shape[0]), "rays_per_step": int(m),
             "value": round(m / ((b + tr) * 1e-3) / 1e6, 1), "unit": "Mrays/s", "ms_per_step": round(b + tr, 4),
             "build_ms": round(b, 4), "trace_ms": round(tr, 4),
-            "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")}}
+            "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")},
+            "trace_tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill")}}
 
 
 def summary_line(line):
@@ -739,6 +741,9 @@ def main():
     ap.add_argument("--step-rays", type=int, default=0,
                     help="profiling: trace only every k-th ray of the headline step (0: all)")
     ap.add_argument("--no-config1", action="store_true", help="skip the mid-size torus step")
+    ap.add_argument("--only-config1", action="store_true", help="only the mid-size torus step (profiling)")
+    ap.add_argument("--tree-global-kernel", type=int, default=None,
+                    help="1: walk tree nodes crossing CTA edges in a separate kernel (default: the library's)")
     ap.add_argument("--trace-refill", type=int, default=None,
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
@@ -781,6 +786,8 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
     if args.trace_leaf_batch is not None:
         ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
+    if args.tree_global_kernel is not None:
+        ctx.set_param(_lib.PARAM_TREE_GLOBAL_KERNEL, args.tree_global_kernel)
 
     def detail(name, rec):
         if rank == 0:
@@ -793,6 +800,9 @@ def main():
         detail("batched", measure_batched(local, args.steps, hbm_peak, peak_kind))
         return 0
     flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)  # 256 MB > L2
+    if args.only_config1:
+        detail("config1", measure_config1(ctx, stream, flush, dev, args.steps))
+        return 0
     if args.only_16m:
         detail("build_16m", measure_build_16m(ctx, lb.Builder(ctx), stream, flush, dev, args.steps, hbm_peak,
                                               peak_kind, args.soup_n, args.soup_span))
@@ -821,6 +831,9 @@ def main():
     hits_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32, device=dev)
     m = prim.shape[0] + bounce.shape[0]
     config = room_config(tris_h, prim_h, bounce_h, world)
+    # the traversal's leaf batching and refill, tuned on a sample of the step's rays
+    trace_tuning = autotune.tune_trace(ctx, bvh, torch.cat([prim[::8], bounce[::8]]),
+                                       key=f"gb300:trace:{WORKLOAD}")
 
     for _ in range(args.warmup):
         builder(tris, into=bvh)
@@ -893,9 +906,11 @@ def main():
         "build": {"ms": round(build_ms, 4), "mprims_s": round(n / (build_ms * 1e-3) / 1e6, 1),
                   "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")}},
         "trace": {"ms": round(trace_ms, 4), "mrays_s": round(m / (trace_ms * 1e-3) / 1e6, 1),
-                  "primary_hit_fraction": round(hit_frac, 4)},
+                  "primary_hit_fraction": round(hit_frac, 4),
+                  "tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill")}},
     }
     detail("build_tuning", tuning)
+    detail("trace_tuning", trace_tuning)
     if args.only_step:
         line["gpu_launches"] = gpu_launches
         line["clocks"] = clk

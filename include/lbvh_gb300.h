@@ -141,6 +141,9 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_BUCKET_SORT_MIN 12    /* keys-only builds of at least this many primitives sort by
                                             buckets of the top 12 code bits (>= 65,536; default 1,500,000) */
 #define LBVH_PARAM_BOUNDS_BLOCKS_PER_SM 13 /* CTAs per SM of the bounds pass, 1..16 (default 4) */
+#define LBVH_PARAM_TREE_GLOBAL_KERNEL 14 /* trees of more than 49,152 primitives: 0 (default) walks the
+                                            nodes crossing CTA edges from the tail of the local tree phase,
+                                            1 in a separate kernel after it */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

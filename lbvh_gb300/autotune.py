@@ -10,6 +10,10 @@ Tunes, on a caller-supplied sample workload:
     (LBVH_PARAM_TRACE_BLOCKS_PER_SM), the ray-refill threshold
     (LBVH_PARAM_TRACE_REFILL) and the leaf-test batching
     (LBVH_PARAM_TRACE_LEAF_BATCH) of the batched trace;
+  * the plain trace (tune_trace), per workload: the leaf-test batching
+    (LBVH_PARAM_TRACE_LEAF_BATCH) and the ray-refill threshold, timed on a
+    sample of the workload's rays -- long rays through loose trees gain from
+    batching the triangle tests of a warp's lanes, short rays lose;
   * the plain build (tune_build), per size class (primitive counts in
     [2^k, 2^(k+1))): the keys-only sort's tile (LBVH_PARAM_SORT_TILE_KEYS:
     1,024 or 4,096 keys), whether the bucket sort runs
@@ -33,7 +37,7 @@ BATCH_RADIX_BITS = (4, 6, 8)
 BATCH_KEYS_PER_THREAD = (4, 8)
 TRACE_BLOCKS_PER_SM = (6, 8)
 TRACE_REFILL = (8, 12, 16)
-TRACE_LEAF_BATCH = (1, 8)
+TRACE_LEAF_BATCH = (1, 4, 8)
 SORT_TILE_KEYS = (1024, 4096)
 BOUNDS_BLOCKS_PER_SM = (2, 4, 8)
 BUCKET_SORT_MIN = 65536  # the smallest size the bucket sort may take
@@ -210,3 +214,34 @@ def tune_build(ctx, tris, reps: int = 5, table_path: str | None = None, force: b
     _store(table, key, best, table_path)
     apply(ctx, best)
     return best
+
+
+def tune_trace(ctx, bvh, rays, key: str, sample: int = 1 << 18, reps: int = 3, table_path: str | None = None,
+               force: bool = False) -> dict:
+    """Best leaf-test batching and refill threshold for tracing `rays` (a
+    device [m, 8] array) against `bvh`, timed on up to `sample` evenly spaced
+    rays; cached under `key`. Returns the setting and applies it."""
+    import torch
+
+    from .api import Traverser
+
+    table = load_table(table_path)
+    if key in table and not force:
+        apply(ctx, table[key])
+        return table[key]
+    stream = torch.cuda.current_stream()
+    step = max(1, int(rays.shape[0]) // sample)
+    part = rays[::step].contiguous()
+    out = torch.empty((part.shape[0], 4), dtype=torch.float32, device=rays.device)
+    trav = Traverser(bvh)
+    ms = {}
+    for leaf in TRACE_LEAF_BATCH:
+        for refill in TRACE_REFILL:
+            apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill})
+            ms[(leaf, refill)] = _time(lambda: trav(part, out=out), stream, reps)
+    leaf, refill = min(ms, key=ms.get)
+    setting = {"trace_leaf_batch": leaf, "trace_refill": refill, "sample_rays": int(part.shape[0]),
+               "trace_ms": {f"{k[0]}x{k[1]}": round(v, 4) for k, v in ms.items()}}
+    _store(table, key, setting, table_path)
+    apply(ctx, setting)
+    return setting

@@ -916,6 +916,50 @@ static_assert(sizeof(PendingNode) == 32, "pending record layout");
 constexpr uint32_t kSlotEmpty = 0xffffffffu;    // no arrival yet
 constexpr uint32_t kSlotComplete = 0xfffffffeu; // both children arrived
 
+// The walk of one pending node [L, R] (box `box`) up through the global
+// epoch-tagged arrival slots: at each parent the first of the two children
+// to arrive parks its far range end and stops, the second completes the
+// parent (its record is published by the release half of this thread's next
+// arrival) and climbs on. Node records the sibling's walk wrote are read
+// after the acquire half of this thread's arrival.
+template<class Leaf>
+__device__ __forceinline__ void
+walk_global(const Leaf& leaf, uint32_t n, const uint32_t* __restrict__ codes, unsigned long long* __restrict__ slots,
+            Node* __restrict__ nodes, BuildState* __restrict__ st, uint32_t epoch, uint32_t L, uint32_t R, Box box)
+{
+  const unsigned long long tag = (unsigned long long)epoch << 32;
+  bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+  for (uint32_t depth = 0;; depth++) {
+    if (depth > kMaxTreeDepth + 2) {
+      atomicOr(&st->error, kErrBadTopology);
+      return;
+    }
+    const uint32_t s = is_left ? R : L - 1;
+    const unsigned long long old = arrive_acq_rel(slots + s, tag | (is_left ? L : R));
+    if (uint32_t(old >> 32) != epoch)
+      return; // first arrival: the sibling completes the parent
+    const uint32_t far = uint32_t(old);
+    const uint32_t LP = is_left ? L : far, RP = is_left ? far : R;
+    const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
+    const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
+    const uint32_t sib = is_left ? cr : cl;
+    Box other;
+    if (sib & kLeafBit)
+      other = leaf(sib & ~kLeafBit);
+    else
+      other = load_node_box(nodes, sib); // published before the sibling's swap, seen after ours
+    box = is_left ? join(box, other) : join(other, box);
+    L = LP;
+    R = RP;
+    if (L == 0 && R == n - 1) {
+      store_node(nodes, 0, box, cl, cr);
+      return;
+    }
+    is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+    store_node(nodes, is_left ? R : L, box, cl, cr);
+  }
+}
+
 template<class Leaf>
 __global__ __launch_bounds__(kTreeThreads) void
 k_tree_local(Leaf leaf,
@@ -924,7 +968,10 @@ k_tree_local(Leaf leaf,
              Node* __restrict__ nodes,
              PendingNode* __restrict__ pending_out,
              uint32_t pending_cap,
-             BuildState* __restrict__ st)
+             BuildState* __restrict__ st,
+             unsigned long long* __restrict__ slots,
+             uint32_t epoch,
+             bool walk_on)
 {
   pdl_begin(); // the predecessor in the stream has finished
   extern __shared__ __align__(32) unsigned char smem[];
@@ -1054,6 +1101,21 @@ k_tree_local(Leaf leaf,
   }
   __syncthreads();
   const uint32_t np = s_npend;
+  if (walk_on) {
+    // The global phase starts here: each pending node walks up through the
+    // global arrival slots at once, so chains across CTA edges overlap the
+    // local phases of the CTAs still to run. This CTA's records were all
+    // written before the barrier above; the fence orders them before the
+    // walk's first release.
+    if (tid == 0 && np > kTreePendingPerBlock)
+      atomicOr(&st->error, kErrBadTopology); // more canonical pieces than a tree can have
+    if (tid < min(np, kTreePendingPerBlock)) {
+      __threadfence();
+      const PendingNode pn = s_pend[tid];
+      walk_global(leaf, n, codes, slots, nodes, st, epoch, pn.L, pn.R, pn.box);
+    }
+    return;
+  }
   if (tid == 0) {
     if (np > kTreePendingPerBlock)
       atomicOr(&st->error, kErrBadTopology); // more canonical pieces than a tree can have
@@ -1087,41 +1149,8 @@ k_tree_global(Leaf leaf,
   if (__ldcg(&st->error) & kErrLookbackTimeout)
     return; // the sort gave up: no tree (the error is reported)
   const PendingNode pn = pending_in[i];
-  uint32_t L = pn.L, R = pn.R;
-  Box box = pn.box;
-  const unsigned long long tag = (unsigned long long)epoch << 32;
-  // records from the local phase are visible at launch; a record this thread
-  // writes is published by the release half of its next arrival
-  bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
-  for (uint32_t depth = 0;; depth++) {
-    if (depth > kMaxTreeDepth + 2) {
-      atomicOr(&st->error, kErrBadTopology);
-      return;
-    }
-    const uint32_t s = is_left ? R : L - 1;
-    const unsigned long long old = arrive_acq_rel(slots + s, tag | (is_left ? L : R));
-    if (uint32_t(old >> 32) != epoch)
-      return; // first arrival: the sibling completes the parent
-    const uint32_t far = uint32_t(old);
-    const uint32_t LP = is_left ? L : far, RP = is_left ? far : R;
-    const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
-    const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
-    const uint32_t sib = is_left ? cr : cl;
-    Box other;
-    if (sib & kLeafBit)
-      other = leaf(sib & ~kLeafBit);
-    else
-      other = load_node_box(nodes, sib); // published before the sibling's swap, seen after ours
-    box = is_left ? join(box, other) : join(other, box);
-    L = LP;
-    R = RP;
-    if (L == 0 && R == n - 1) {
-      store_node(nodes, 0, box, cl, cr);
-      return;
-    }
-    is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
-    store_node(nodes, is_left ? R : L, box, cl, cr);
-  }
+  // records from the local phase are visible at launch
+  walk_global(leaf, n, codes, slots, nodes, st, epoch, pn.L, pn.R, pn.box);
 }
 
 // The global phase for trees whose n - 1 split positions fit in shared
@@ -1451,10 +1480,13 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
   }
   const uint32_t blocks = ceil_div_u32(n, kTreeBlock);
   const uint32_t cap = blocks * kTreePendingPerBlock;
+  // trees beyond the one-CTA global phase walk their CTA edges from the
+  // local phase's tail, unless the context asks for the separate kernel
+  const bool walk_on = blocks > 1 && n > kTreeGlobalCtaMaxPrims && b.tree_walk != 1;
   CUDA_TRY(launch_pdl(k_tree_local<Leaf>, blocks, kTreeThreads, kTreeSmem, s, leaf, n, b.keys_a, nodes,
-                      reinterpret_cast<PendingNode*>(b.pending), cap, b.state));
-  if (blocks == 1)
-    return cudaGetLastError(); // the whole tree was built in the one CTA
+                      reinterpret_cast<PendingNode*>(b.pending), cap, b.state, b.slots, epoch, walk_on));
+  if (blocks == 1 || walk_on)
+    return cudaGetLastError(); // the whole tree was built in the one CTA, or by the walks
   if (n <= kTreeGlobalCtaMaxPrims) {
     CUDA_TRY(launch_pdl(k_tree_global_cta<Leaf>, 1, kTreeGlobalCtaThreads, size_t(4) * (n - 1), s, leaf, n, b.keys_a,
                         nodes, reinterpret_cast<const PendingNode*>(b.pending), cap, b.state));
