@@ -742,8 +742,8 @@ def main():
                     help="profiling: trace only every k-th ray of the headline step (0: all)")
     ap.add_argument("--no-config1", action="store_true", help="skip the mid-size torus step")
     ap.add_argument("--only-config1", action="store_true", help="only the mid-size torus step (profiling)")
-    ap.add_argument("--tree-global-kernel", type=int, default=None,
-                    help="1: walk tree nodes crossing CTA edges in a separate kernel (default: the library's)")
+    ap.add_argument("--tree-walk-fused", type=int, default=None,
+                    help="1: walk tree nodes crossing CTA edges from the local phase's tail (default: the library's)")
     ap.add_argument("--trace-refill", type=int, default=None,
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
@@ -786,8 +786,8 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
     if args.trace_leaf_batch is not None:
         ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
-    if args.tree_global_kernel is not None:
-        ctx.set_param(_lib.PARAM_TREE_GLOBAL_KERNEL, args.tree_global_kernel)
+    if args.tree_walk_fused is not None:
+        ctx.set_param(_lib.PARAM_TREE_WALK_FUSED, args.tree_walk_fused)
 
     def detail(name, rec):
         if rank == 0:

@@ -131,8 +131,9 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             traversal then reaches host memory over the CPU-GPU link);
                                             pageable host memory is always copied */
 #define LBVH_PARAM_TRACE_LEAF_BATCH 8    /* lanes of a traversal warp with pending leaf-triangle tests
-                                            before the warp runs them together, 1..32 (1: each lane tests
-                                            its triangles right after its visit); results do not change */
+                                            before the warp runs them together, 1..32 (1, the default: each
+                                            lane tests its triangles right after its visit); results do not
+                                            change; long rays through loose trees gain from 4-8 */
 #define LBVH_PARAM_BATCH_RADIX_BITS 9     /* digit width of the batched build's CTA-local radix sort: 4, 6
                                             or 8 bits (8, 5 or 4 passes over the 30-bit codes) */
 #define LBVH_PARAM_BATCH_KEYS_PER_THREAD 10 /* keys per thread in each chunk that sort ranks: 4 or 8 */
@@ -141,9 +142,9 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_BUCKET_SORT_MIN 12    /* keys-only builds of at least this many primitives sort by
                                             buckets of the top 12 code bits (>= 65,536; default 1,500,000) */
 #define LBVH_PARAM_BOUNDS_BLOCKS_PER_SM 13 /* CTAs per SM of the bounds pass, 1..16 (default 4) */
-#define LBVH_PARAM_TREE_GLOBAL_KERNEL 14 /* trees of more than 49,152 primitives: 0 (default) walks the
-                                            nodes crossing CTA edges from the tail of the local tree phase,
-                                            1 in a separate kernel after it */
+#define LBVH_PARAM_TREE_WALK_FUSED 14    /* trees of more than 49,152 primitives: 0 (default) walks the
+                                            nodes crossing CTA edges in a separate kernel after the local
+                                            tree phase, 1 from each CTA's tail of that phase */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

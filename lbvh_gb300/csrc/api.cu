@@ -63,7 +63,7 @@ struct lbvh_ctx
   uint32_t tile_keys = 0;          // keys-only sort tile (0: by size)
   uint32_t msd_min = kMsdMinPrims; // keys-only builds from this size use the bucket sort
   uint32_t bounds_per_sm = 4;      // bounds-pass CTAs per SM
-  uint32_t tree_walk = 0;          // 0: CTA-edge walks fused into the local tree phase, 1: separate kernel
+  uint32_t walk_fused = 0;         // 1: CTA-edge walks from the local tree phase's tail, 0: separate kernel
   DevBuf batch_ws;                 // batched build: codes, boxes, slots
   uint32_t epoch = 0;          // look-back epoch of the last sort pass
   char msg[512] = { 0 };
@@ -341,7 +341,7 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
   const bool sorted_leaves = flags & LBVH_BUILD_SORTED_LEAVES;
   b.msd = !keep && !sorted_leaves && nn >= c->msd_min; // keys-only sort of a large build
   b.tile_keys = c->tile_keys;
-  b.tree_walk = c->tree_walk;
+  b.walk_fused = c->walk_fused;
   if (b.msd) {
     // ranges of at least one partition tile, a few per SM; their count rows
     // (ranges x 16 KB <= 2n + 16 KB) live in vals_a, unused by keys-only sorts
@@ -689,11 +689,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "bounds CTAs per SM %d outside [1, %u]", value, kMaxBoundsBlocksPerSm);
       c->bounds_per_sm = uint32_t(value);
       return LBVH_OK;
-    case LBVH_PARAM_TREE_GLOBAL_KERNEL:
+    case LBVH_PARAM_TREE_WALK_FUSED:
       if (value < 0 || value > 1)
-        return fail(c, LBVH_ERR_INVALID_ARG, "tree global kernel %d is not 0 or 1", value);
-      c->tree_walk = uint32_t(value);
-      c->bufs.tree_walk = uint32_t(value);
+        return fail(c, LBVH_ERR_INVALID_ARG, "fused tree walk %d is not 0 or 1", value);
+      c->walk_fused = uint32_t(value);
+      c->bufs.walk_fused = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
       if (value < 1 || value > (1 << 24))

@@ -1480,9 +1480,9 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
   }
   const uint32_t blocks = ceil_div_u32(n, kTreeBlock);
   const uint32_t cap = blocks * kTreePendingPerBlock;
-  // trees beyond the one-CTA global phase walk their CTA edges from the
-  // local phase's tail, unless the context asks for the separate kernel
-  const bool walk_on = blocks > 1 && n > kTreeGlobalCtaMaxPrims && b.tree_walk != 1;
+  // trees beyond the one-CTA global phase walk their CTA edges in a
+  // separate kernel, or (when the context asks) from the local phase's tail
+  const bool walk_on = blocks > 1 && n > kTreeGlobalCtaMaxPrims && b.walk_fused == 1;
   CUDA_TRY(launch_pdl(k_tree_local<Leaf>, blocks, kTreeThreads, kTreeSmem, s, leaf, n, b.keys_a, nodes,
                       reinterpret_cast<PendingNode*>(b.pending), cap, b.state, b.slots, epoch, walk_on));
   if (blocks == 1 || walk_on)

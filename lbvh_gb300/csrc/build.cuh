@@ -108,8 +108,8 @@ struct BuildBuffers
   uint32_t* top_rows;             // bucket sort: msd_ranges x kTopBuckets counts (in vals_a)
   uint32_t tile_keys;             // keys-only onesweep tile: 0 automatic (kSmallTile up to
                                   // kSmallTileMaxPrims codes, else kSortTile), or kSmallTile / kSortTile
-  uint32_t tree_walk;             // trees beyond kTreeGlobalCtaMaxPrims: 0 walk CTA edges from the
-                                  // local phase's tail, 1 in a separate global kernel
+  uint32_t walk_fused;            // trees beyond kTreeGlobalCtaMaxPrims: 0 walk the nodes crossing CTA
+                                  // edges in a separate global kernel, 1 from the local phase's tail
   uint32_t spin_limit;            // look-back polls before a wait gives up (0: kSpinLimit)
   uint32_t wait_xor;              // test only: nonzero makes every look-back wait for a tag no
                                   // tile publishes, so each wait runs out (0 in normal use)

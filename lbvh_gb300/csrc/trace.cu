@@ -232,7 +232,10 @@ constexpr uint32_t kHitDirect = kHitRing; // a ray whose hit is written directly
 #define LBVH_TRACE_MIN_BLOCKS 8 // resident CTAs per SM the register budget is set for
 #endif
 
-template<bool kCounts, bool kBatch, bool kHostHits = false>
+// kLeafBatch: the leaf triangles of a visit are tested when leaf_batch of
+// the warp's lanes have some pending (see below); otherwise right after the
+// visit, by the lane alone.
+template<bool kCounts, bool kBatch, bool kHostHits = false, bool kLeafBatch = false>
 __global__ __launch_bounds__(kTraceThreads, LBVH_TRACE_MIN_BLOCKS) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
@@ -417,11 +420,30 @@ k_trace(const WideNode* __restrict__ wnodes,
         if (!(right & kLeafBit))
           rhit = box_test(r, B.z, B.w, C.x, C.y, C.z, C.w, rt);
       }
-      // leaf children: tested below, left before right, before this lane's
-      // next pop (so its cull test sees their hits, as in the reference)
+      // leaf children: tested left before right, before this lane's next
+      // pop (so its cull test sees their hits, as in the reference) -- here,
+      // or with the warp's other pending lanes below
       leaf_l = (left & kLeafBit) ? (left & ~kLeafBit) : kMiss;
       leaf_r = (right & kLeafBit) ? (right & ~kLeafBit) : kMiss;
-      pend = ((left | right) & kLeafBit) != 0;
+      if (kLeafBatch) {
+        pend = ((left | right) & kLeafBit) != 0;
+      } else if ((left | right) & kLeafBit) {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+          const uint32_t p = k == 0 ? leaf_l : leaf_r;
+          if (p != kMiss) {
+            float t, u, v;
+            if (kCounts)
+              ct++;
+            if (tri_test(r, tris + tb, p, t, u, v) && t < best_t) {
+              best_p = p;
+              best_t = t;
+              best_u = u;
+              best_v = v;
+            }
+          }
+        }
+      }
       // pushes; the last one pushed stays in registers as the next pop
       has_cur = false;
       if (lhit && rhit) {
@@ -447,7 +469,7 @@ k_trace(const WideNode* __restrict__ wnodes,
     // it, so a lane with pending triangles sits out node visits until
     // leaf_batch lanes are pending, or until no lane is left to visit; each
     // ray still visits, tests and pops in the reference's order. ----
-    const uint32_t pmask = __ballot_sync(0xffffffffu, pend);
+    const uint32_t pmask = kLeafBatch ? __ballot_sync(0xffffffffu, pend) : 0u;
     if (pmask && (uint32_t(__popc(pmask)) >= leaf_batch || __ballot_sync(0xffffffffu, busy && !pend) == 0)) {
       if (pend) {
 #pragma unroll
@@ -542,16 +564,27 @@ launch_trace_tris(const WideNode* wnodes,
   const uint32_t blocks = want < cap ? want : cap;
   const float4* r4 = reinterpret_cast<const float4*>(rays);
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + n_nodes);
-  if (n_box && n_tri)
-    k_trace<true, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, n_box, n_tri,
-                                                          ray_counter, wide, p.refill, p.leaf_batch, nullptr, nullptr, 0);
-  else if (host_hits)
-    k_trace<false, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
-                                                                 nullptr, ray_counter, wide, p.refill, p.leaf_batch,
-                                                                 nullptr, nullptr, 0);
-  else
-    k_trace<false, false><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
-                                                           ray_counter, wide, p.refill, p.leaf_batch, nullptr, nullptr, 0);
+  // leaf batching pays for long rays in loose trees (the tuner decides)
+  auto go = [&](auto kernel, uint32_t* nb, uint32_t* nt) {
+    kernel<<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nb, nt, ray_counter, wide, p.refill,
+                                           p.leaf_batch, nullptr, nullptr, 0);
+  };
+  const bool counts = n_box && n_tri;
+  if (p.leaf_batch > 1) {
+    if (counts)
+      go(k_trace<true, false, false, true>, n_box, n_tri);
+    else if (host_hits)
+      go(k_trace<false, false, true, true>, nullptr, nullptr);
+    else
+      go(k_trace<false, false, false, true>, nullptr, nullptr);
+  } else {
+    if (counts)
+      go(k_trace<true, false>, n_box, n_tri);
+    else if (host_hits)
+      go(k_trace<false, false, true>, nullptr, nullptr);
+    else
+      go(k_trace<false, false>, nullptr, nullptr);
+  }
   return cudaGetLastError();
 }
 
@@ -776,9 +809,15 @@ launch_batch_trace(const WideNode* wnodes,
   const uint32_t cap = uint32_t(num_sms) * p.blocks_per_sm;
   const uint32_t blocks = want < cap ? want : cap;
   const uint32_t* wide = reinterpret_cast<const uint32_t*>(wnodes + total_nodes);
-  k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, reinterpret_cast<const float4*>(rays),
-                                                        m, hits, nullptr, nullptr, ray_counter, wide, p.refill,
-                                                        p.leaf_batch, off, roff, n_meshes);
+  const float4* r4 = reinterpret_cast<const float4*>(rays);
+  if (p.leaf_batch > 1)
+    k_trace<false, true, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
+                                                                      nullptr, ray_counter, wide, p.refill,
+                                                                      p.leaf_batch, off, roff, n_meshes);
+  else
+    k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
+                                                          ray_counter, wide, p.refill, p.leaf_batch, off, roff,
+                                                          n_meshes);
   return cudaGetLastError();
 }
 

@@ -13,7 +13,7 @@ struct TraceParams
 {
   uint32_t blocks_per_sm = 8; // resident 128-thread blocks per SM
   uint32_t refill = 12;       // idle lanes at which a warp takes new rays
-  uint32_t leaf_batch = 8;    // lanes with pending triangle tests before a warp runs them (1: at once)
+  uint32_t leaf_batch = 1;    // lanes with pending triangle tests before a warp runs them (1: at once)
 };
 
 // Traversal copy of an internal node: both children's boxes plus the child

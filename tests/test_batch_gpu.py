@@ -75,7 +75,16 @@ def test_batch_radix_width_and_keys_per_thread(ctx, port, bits, items, sorted_le
         ctx.set_param(_lib.PARAM_BATCH_KEYS_PER_THREAD, 6)
 
 
-def test_batch_trace_matches_oracle(ctx, port):
+@pytest.mark.parametrize("leaf_batch", [1, 8])
+def test_batch_trace_matches_oracle(ctx, port, leaf_batch):
+    ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, leaf_batch)
+    try:
+        _batch_trace_matches_oracle(ctx, port)
+    finally:
+        ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, 1)
+
+
+def _batch_trace_matches_oracle(ctx, port):
     meshes, tris, off = make_batch([2, 17, 500, 3000, 40000], 7)
     b = lb.Batch(ctx).build(dev(tris), off)
     rays, roff = [], [0]

@@ -204,8 +204,8 @@ def test_sort_and_bounds_parameters(lib_built, port, tile, bucket_min, bounds):
             c.set_param(param, bad)
 
 
-@pytest.mark.parametrize("separate", [0, 1])
-def test_tree_global_phase_fused_or_separate(lib_built, port, separate):
+@pytest.mark.parametrize("fused", [0, 1])
+def test_tree_global_phase_fused_or_separate(lib_built, port, fused):
     """The nodes crossing CTA edges, walked from the local phase's tail or
     by a separate kernel afterwards, give the reference's nodes (and so do
     builds small enough for the one-CTA global phase), for builds and for
@@ -213,10 +213,10 @@ def test_tree_global_phase_fused_or_separate(lib_built, port, separate):
     from lbvh_gb300 import _lib
 
     c = lb.Context()
-    c.set_param(_lib.PARAM_TREE_GLOBAL_KERNEL, separate)
+    c.set_param(_lib.PARAM_TREE_WALK_FUSED, fused)
     for n in (20_000, 49_153, 300_007):
         t = scenes.soup(n, 70 + n % 5)
-        assert nodes_equal(lb.Builder(c)(dev(t)).nodes(), port.build(t, 16)), (separate, n)
+        assert nodes_equal(lb.Builder(c)(dev(t)).nodes(), port.build(t, 16)), (fused, n)
     room = scenes.room_scene(seed=21)
     assert nodes_equal(lb.Builder(c)(dev(room)).nodes(), port.build(room, 16))
     t = scenes.soup(600_000, 77)  # refits from 2^19 primitives rerun the tree phase
@@ -225,7 +225,7 @@ def test_tree_global_phase_fused_or_separate(lib_built, port, separate):
     b.refit(dev(t2))
     assert nodes_equal(b.nodes(), port.refit(port.build(t, 16), t2))
     with pytest.raises(ValueError):
-        c.set_param(_lib.PARAM_TREE_GLOBAL_KERNEL, 2)
+        c.set_param(_lib.PARAM_TREE_WALK_FUSED, 2)
 
 
 def test_full_size_16m_build_parity(ctx, port):
