@@ -34,6 +34,19 @@ struct RayCtx
   bool fast;          // no slab value can be NaN: min/max may use fminf/fmaxf
 };
 
+// 1 / x correctly rounded. IEEE 754 gives a correctly rounded reciprocal
+// and a correctly rounded division of 1 by x the same bits, so this is the
+// reference's `1 / x`.
+__device__ __forceinline__ float
+rcp_rn(float x)
+{
+#ifdef LBVH_TRACE_DIV_RCP
+  return fdiv(1.0f, x);
+#else
+  return __frcp_rn(x);
+#endif
+}
+
 // Packed IEEE single-precision add on a pair (elementwise, round to
 // nearest): each half is exactly what __fadd_rn gives. Only the add is
 // packed. The products feeding it are scalar __fmul_rn: the assembler may
@@ -82,7 +95,7 @@ make_ray(const float4 a, const float4 b)
   r.tmin = b.z;
   r.tmax = b.w;
   // make_accel_ray, lbvh.h:991-1010
-  const float rx = fdiv(1.0f, r.dx), ry = fdiv(1.0f, r.dy), rz = fdiv(1.0f, r.dz);
+  const float rx = rcp_rn(r.dx), ry = rcp_rn(r.dy), rz = rcp_rn(r.dz);
   const float ix = fmul(-r.px, rx), iy = fmul(-r.py, ry), iz = fmul(-r.pz, rz);
   r.rxy = make_float2(rx, ry);
   r.ixy = make_float2(ix, iy);
@@ -163,7 +176,7 @@ tri_test(const RayCtx& r, const Tri* __restrict__ tris, uint32_t p, float& t, fl
   const float qx = fsub(fmul(r.dy, cz), fmul(r.dz, cy));
   const float qy = fsub(fmul(r.dz, cx), fmul(r.dx, cz));
   const float qz = fsub(fmul(r.dx, cy), fmul(r.dy, cx));
-  const float inv_det = fdiv(1.0f, dot3(nx, ny, nz, r.dx, r.dy, r.dz));
+  const float inv_det = rcp_rn(dot3(nx, ny, nz, r.dx, r.dy, r.dz));
   u = fmul(dot3(qx, qy, qz, e1x, e1y, e1z), inv_det);
   v = fmul(dot3(qx, qy, qz, e0x, e0y, e0z), inv_det);
   const float w = fsub(fsub(1.0f, u), v);
@@ -231,12 +244,15 @@ constexpr uint32_t kHitDirect = kHitRing; // a ray whose hit is written directly
 #ifndef LBVH_TRACE_MIN_BLOCKS
 #define LBVH_TRACE_MIN_BLOCKS 8 // resident CTAs per SM the register budget is set for
 #endif
+#ifndef LBVH_TRACE_MIN_BLOCKS_LEAF
+#define LBVH_TRACE_MIN_BLOCKS_LEAF 8 // the same for the leaf-batching variant
+#endif
 
 // kLeafBatch: the leaf triangles of a visit are tested when leaf_batch of
 // the warp's lanes have some pending (see below); otherwise right after the
 // visit, by the lane alone.
 template<bool kCounts, bool kBatch, bool kHostHits = false, bool kLeafBatch = false>
-__global__ __launch_bounds__(kTraceThreads, LBVH_TRACE_MIN_BLOCKS) void
+__global__ __launch_bounds__(kTraceThreads, kLeafBatch ? LBVH_TRACE_MIN_BLOCKS_LEAF : LBVH_TRACE_MIN_BLOCKS) void
 k_trace(const WideNode* __restrict__ wnodes,
         const Tri* __restrict__ tris,
         const uint32_t* __restrict__ leaf_prim,
