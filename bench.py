@@ -696,7 +696,7 @@ def measure_config1(ctx, stream, flush, dev, steps):
             "value": round(m / ((b + tr) * 1e-3) / 1e6, 1), "unit": "Mrays/s", "ms_per_step": round(b + tr, 4),
             "build_ms": round(b, 4), "trace_ms": round(tr, 4),
             "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")},
-            "trace_tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill")}}
+            "trace_tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill", "trace_blocks_per_sm")}}
 
 
 def summary_line(line):
@@ -748,6 +748,8 @@ def main():
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
                     help="resident traversal CTAs per SM (default: the library's)")
+    ap.add_argument("--trace-ray-order", type=int, default=None,
+                    help="1: each SM traces a contiguous segment of the rays first (default: the library's)")
     ap.add_argument("--trace-leaf-batch", type=int, default=None,
                     help="lanes with pending triangle tests before a traversal warp runs them (default: the library's)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
@@ -786,6 +788,8 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
     if args.trace_leaf_batch is not None:
         ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
+    if args.trace_ray_order is not None:
+        ctx.set_param(_lib.PARAM_TRACE_RAY_ORDER, args.trace_ray_order)
     if args.tree_walk_fused is not None:
         ctx.set_param(_lib.PARAM_TREE_WALK_FUSED, args.tree_walk_fused)
 
@@ -907,7 +911,7 @@ def main():
                   "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")}},
         "trace": {"ms": round(trace_ms, 4), "mrays_s": round(m / (trace_ms * 1e-3) / 1e6, 1),
                   "primary_hit_fraction": round(hit_frac, 4),
-                  "tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill")}},
+                  "tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill", "trace_blocks_per_sm")}},
     }
     detail("build_tuning", tuning)
     detail("trace_tuning", trace_tuning)

@@ -38,6 +38,7 @@ BATCH_KEYS_PER_THREAD = (4, 8)
 TRACE_BLOCKS_PER_SM = (6, 8)
 TRACE_REFILL = (8, 12, 16)
 TRACE_LEAF_BATCH = (1, 4, 8)
+TRACE_GRID = (8, 9)  # CTAs per SM; the leaf-batching variant is compiled to fit 9
 SORT_TILE_KEYS = (1024, 4096)
 BOUNDS_BLOCKS_PER_SM = (2, 4, 8)
 BUCKET_SORT_MIN = 65536  # the smallest size the bucket sort may take
@@ -237,11 +238,13 @@ def tune_trace(ctx, bvh, rays, key: str, sample: int = 1 << 18, reps: int = 3, t
     ms = {}
     for leaf in TRACE_LEAF_BATCH:
         for refill in TRACE_REFILL:
-            apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill})
-            ms[(leaf, refill)] = _time(lambda: trav(part, out=out), stream, reps)
-    leaf, refill = min(ms, key=ms.get)
-    setting = {"trace_leaf_batch": leaf, "trace_refill": refill, "sample_rays": int(part.shape[0]),
-               "trace_ms": {f"{k[0]}x{k[1]}": round(v, 4) for k, v in ms.items()}}
+            for grid in TRACE_GRID if leaf > 1 else TRACE_GRID[:1]:
+                apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid})
+                ms[(leaf, refill, grid)] = _time(lambda: trav(part, out=out), stream, reps)
+    leaf, refill, grid = min(ms, key=ms.get)
+    setting = {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid,
+               "sample_rays": int(part.shape[0]),
+               "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in ms.items()}}
     _store(table, key, setting, table_path)
     apply(ctx, setting)
     return setting
