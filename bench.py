@@ -748,8 +748,6 @@ def main():
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
                     help="resident traversal CTAs per SM (default: the library's)")
-    ap.add_argument("--trace-ray-order", type=int, default=None,
-                    help="1: each SM traces a contiguous segment of the rays first (default: the library's)")
     ap.add_argument("--trace-leaf-batch", type=int, default=None,
                     help="lanes with pending triangle tests before a traversal warp runs them (default: the library's)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
@@ -788,8 +786,6 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
     if args.trace_leaf_batch is not None:
         ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
-    if args.trace_ray_order is not None:
-        ctx.set_param(_lib.PARAM_TRACE_RAY_ORDER, args.trace_ray_order)
     if args.tree_walk_fused is not None:
         ctx.set_param(_lib.PARAM_TREE_WALK_FUSED, args.tree_walk_fused)
 
@@ -835,9 +831,9 @@ def main():
     hits_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32, device=dev)
     m = prim.shape[0] + bounce.shape[0]
     config = room_config(tris_h, prim_h, bounce_h, world)
-    # the traversal's leaf batching and refill, tuned on a sample of the step's rays
-    trace_tuning = autotune.tune_trace(ctx, bvh, torch.cat([prim[::8], bounce[::8]]),
-                                       key=f"gb300:trace:{WORKLOAD}")
+    # the traversal's leaf batching, refill and grid, tuned on the step's own rays
+    # (a sparse sample neither fills the GPU nor keeps the rays' coherence)
+    trace_tuning = autotune.tune_trace(ctx, bvh, torch.cat([prim, bounce]), key=f"gb300:trace:{WORKLOAD}")
 
     for _ in range(args.warmup):
         builder(tris, into=bvh)

@@ -145,9 +145,6 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_TREE_WALK_FUSED 14    /* trees of more than 49,152 primitives: 0 (default) walks the
                                             nodes crossing CTA edges in a separate kernel after the local
                                             tree phase, 1 from each CTA's tail of that phase */
-#define LBVH_PARAM_TRACE_RAY_ORDER 15    /* how traversal warps take rays: 0 (default) in 32-ray batches from
-                                            one counter; 1 each SM first from its own contiguous segment of
-                                            the rays (neighbouring rays on one SM), then from the others' */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

@@ -217,11 +217,15 @@ def tune_build(ctx, tris, reps: int = 5, table_path: str | None = None, force: b
     return best
 
 
-def tune_trace(ctx, bvh, rays, key: str, sample: int = 1 << 18, reps: int = 3, table_path: str | None = None,
+def tune_trace(ctx, bvh, rays, key: str, sample: int | None = None, reps: int = 2, table_path: str | None = None,
                force: bool = False) -> dict:
-    """Best leaf-test batching and refill threshold for tracing `rays` (a
-    device [m, 8] array) against `bvh`, timed on up to `sample` evenly spaced
-    rays; cached under `key`. Returns the setting and applies it."""
+    """Best leaf-test batching, refill threshold and grid for tracing `rays`
+    (a device [m, 8] array) against `bvh`; cached under `key`. Timed on all
+    the rays by default: a sample too small to fill the GPU, or too sparse
+    to keep neighbouring rays together, favours other settings than the
+    full workload does. `sample` times about that many rays instead, taken
+    as evenly spaced runs of 4,096 consecutive rays. Returns the setting and
+    applies it."""
     import torch
 
     from .api import Traverser
@@ -231,8 +235,13 @@ def tune_trace(ctx, bvh, rays, key: str, sample: int = 1 << 18, reps: int = 3, t
         apply(ctx, table[key])
         return table[key]
     stream = torch.cuda.current_stream()
-    step = max(1, int(rays.shape[0]) // sample)
-    part = rays[::step].contiguous()
+    m = int(rays.shape[0])
+    if sample is None or sample >= m:
+        part = rays
+    else:
+        run = 4096
+        starts = np.linspace(0, m - run, max(1, sample // run)).astype(np.int64) if m > run else np.zeros(1, np.int64)
+        part = torch.cat([rays[int(a):int(a) + run] for a in starts]).contiguous()
     out = torch.empty((part.shape[0], 4), dtype=torch.float32, device=rays.device)
     trav = Traverser(bvh)
     ms = {}

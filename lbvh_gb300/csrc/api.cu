@@ -555,7 +555,7 @@ lbvh_ctx_create(int device, void* stream, lbvh_ctx** out)
     return bail(e);
   if ((e = cudaMallocHost(&c->h_err, 64)) != cudaSuccess)
     return bail(e);
-  if ((e = cudaMalloc(&c->ray_counter, kRayCounterBytes)) != cudaSuccess)
+  if ((e = cudaMalloc(&c->ray_counter, 256)) != cudaSuccess)
     return bail(e);
   *out = c;
   return LBVH_OK;
@@ -694,11 +694,6 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "fused tree walk %d is not 0 or 1", value);
       c->walk_fused = uint32_t(value);
       c->bufs.walk_fused = uint32_t(value);
-      return LBVH_OK;
-    case LBVH_PARAM_TRACE_RAY_ORDER:
-      if (value < 0 || value > 1)
-        return fail(c, LBVH_ERR_INVALID_ARG, "ray order %d is not 0 or 1", value);
-      c->trace.ray_order = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_LOOKBACK_SPIN_LIMIT:
       if (value < 1 || value > (1 << 24))

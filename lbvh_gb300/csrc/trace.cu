@@ -225,31 +225,6 @@ k_repack(const Node* __restrict__ nodes, uint32_t n_nodes, WideNode* __restrict_
 
 // ---------------------------------------------------------------------------
 
-// The next 32-ray batch of a warp under ray order 1: the rays are cut into
-// `count` segments of `len` rays (a multiple of 32), segment v holding
-// [v * len, min((v + 1) * len, m)); a warp draws from its SM's segment
-// (`home`) and, once that is empty, from the following ones in turn
-// (`cur`: how many it has found empty). Returns m when every segment is
-// empty. Called by one lane of the warp.
-__device__ __forceinline__ uint32_t
-fetch_segment(uint32_t* segs, uint32_t m, uint32_t home, uint32_t count, uint32_t len, uint32_t& cur)
-{
-  while (cur < count) {
-    const uint32_t v = home + cur < count ? home + cur : home + cur - count;
-    const uint32_t lo = v * len;
-    if (lo < m) {
-      const uint32_t n = min(len, m - lo);
-      if (*reinterpret_cast<volatile uint32_t*>(segs + v) < n) { // an empty segment costs no atomic
-        const uint32_t old = atomicAdd(segs + v, 32u);
-        if (old < n)
-          return lo + old;
-      }
-    }
-    cur++;
-  }
-  return m;
-}
-
 // kBatch: rays [roff[k], roff[k + 1]) belong to mesh k, whose nodes start at
 // moff[k] - k and whose triangles start at moff[k] (local indices inside).
 //
@@ -286,7 +261,6 @@ k_trace(const WideNode* __restrict__ wnodes,
         const uint32_t* __restrict__ wide,
         uint32_t refill,
         uint32_t leaf_batch,
-        uint32_t ray_order,
         const uint32_t* __restrict__ moff,
         const uint32_t* __restrict__ roff,
         uint32_t n_meshes)
@@ -316,16 +290,6 @@ k_trace(const WideNode* __restrict__ wnodes,
   // the warp's current batch of 32 ray ids (warp-uniform state)
   uint32_t batch = 0, batch_left = 0;
   bool no_more = false; // the last batch fetched reached the end of the rays
-  // ray order 1: this SM's segment of the rays (see fetch_segment)
-  const bool by_segment = !kBatch && ray_order == 1;
-  uint32_t seg_home = 0, seg_count = 1, seg_len = 0, seg_cur = 0;
-  if (by_segment) {
-    asm("mov.u32 %0, %%smid;" : "=r"(seg_home));
-    asm("mov.u32 %0, %%nsmid;" : "=r"(seg_count));
-    seg_count = seg_count < 1 ? 1 : (seg_count > kMaxRaySegments ? kMaxRaySegments : seg_count);
-    seg_home %= seg_count;
-    seg_len = (ceil_div_u32(ceil_div_u32(m, seg_count), 32u)) * 32u;
-  }
 
   // kHostHits: per warp, kHitRing staged batches {hits, first ray, rays left}
   constexpr int kWarps = kTraceThreads / 32;
@@ -382,10 +346,9 @@ k_trace(const WideNode* __restrict__ wnodes,
         if (got < want && !no_more) {
           uint32_t nb = 0;
           if (lane == 0)
-            nb = by_segment ? fetch_segment(ray_counter + kRaySegBase, m, seg_home, seg_count, seg_len, seg_cur)
-                            : atomicAdd(ray_counter, 32u);
+            nb = atomicAdd(ray_counter, 32u);
           nb = __shfl_sync(0xffffffffu, nb, 0);
-          no_more = by_segment ? nb >= m : nb + 32 >= m;
+          no_more = nb + 32 >= m;
           extra_base = nb;
           batch = nb;
           batch_left = 32 - (want - got);
@@ -605,8 +568,6 @@ launch_trace_tris(const WideNode* wnodes,
   if (m == 0)
     return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(ray_counter, 0, 4, s);
-  if (e == cudaSuccess && p.ray_order == 1)
-    e = cudaMemsetAsync(ray_counter + kRaySegBase, 0, 4 * kMaxRaySegments, s);
   if (e != cudaSuccess)
     return e;
   // persistent grid: enough resident warps per SM, never more than the rays
@@ -618,7 +579,7 @@ launch_trace_tris(const WideNode* wnodes,
   // leaf batching pays for long rays in loose trees (the tuner decides)
   auto go = [&](auto kernel, uint32_t* nb, uint32_t* nt) {
     kernel<<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nb, nt, ray_counter, wide, p.refill,
-                                           p.leaf_batch, p.ray_order, nullptr, nullptr, 0);
+                                           p.leaf_batch, nullptr, nullptr, 0);
   };
   const bool counts = n_box && n_tri;
   if (p.leaf_batch > 1) {
@@ -864,11 +825,11 @@ launch_batch_trace(const WideNode* wnodes,
   if (p.leaf_batch > 1)
     k_trace<false, true, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
                                                                       nullptr, ray_counter, wide, p.refill,
-                                                                      p.leaf_batch, 0u, off, roff, n_meshes);
+                                                                      p.leaf_batch, off, roff, n_meshes);
   else
     k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
-                                                          ray_counter, wide, p.refill, p.leaf_batch, 0u, off,
-                                                          roff, n_meshes);
+                                                          ray_counter, wide, p.refill, p.leaf_batch, off, roff,
+                                                          n_meshes);
   return cudaGetLastError();
 }
 

@@ -7,12 +7,6 @@ namespace lbvh_gb300 {
 
 constexpr int kTraceThreads = 128;
 constexpr uint32_t kStackSize = 128; // traversal_stack<scalar, 128>, lbvh.h:1874
-// The ray dispenser (a context's 4-byte-word buffer): word 0 the global
-// counter, word 8 the batched build's mesh queue, words kRaySegBase.. the
-// per-SM segment counters of TraceParams::ray_order 1.
-constexpr uint32_t kRaySegBase = 64;
-constexpr uint32_t kMaxRaySegments = 512;
-constexpr size_t kRayCounterBytes = 4 * (kRaySegBase + kMaxRaySegments);
 
 // Launch shape of the persistent traversal kernel (set per context).
 struct TraceParams
@@ -20,8 +14,6 @@ struct TraceParams
   uint32_t blocks_per_sm = 8; // resident 128-thread blocks per SM
   uint32_t refill = 12;       // idle lanes at which a warp takes new rays
   uint32_t leaf_batch = 1;    // lanes with pending triangle tests before a warp runs them (1: at once)
-  uint32_t ray_order = 0;     // 0: warps draw 32-ray batches from one counter; 1: each SM from its own
-                              // contiguous segment of the rays first, then from the others'
 };
 
 // Traversal copy of an internal node: both children's boxes plus the child

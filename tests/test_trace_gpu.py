@@ -263,30 +263,3 @@ def test_leaf_batch_settings_match(ctx, port, leaf_batch):
     assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
     with pytest.raises(ValueError):
         c.set_param(_lib.PARAM_TRACE_LEAF_BATCH, 0)
-
-
-@pytest.mark.parametrize("ray_order", [0, 1])
-def test_ray_order_settings_match(ctx, port, ray_order):
-    """Warps drawing rays from one counter or from per-SM segments (with
-    stealing) trace every ray exactly once with the reference's result:
-    ray counts below one batch, not a multiple of 32, and the room slice;
-    per-ray test counts included."""
-    from lbvh_gb300 import _lib
-
-    c = lb.Context()
-    c.set_param(_lib.PARAM_TRACE_RAY_ORDER, ray_order)
-    t = scenes.soup(968, seed=1)
-    nodes = port.build(t, 8)
-    bvh = lb.Builder(c)(dev(t))
-    for m in (1, 5, 33, 1000, 65_537):
-        rays = np.ascontiguousarray(scenes.incoherent_rays(t, m, 9 + m))
-        want, nb, nt = port.trace(nodes, t, rays, 16, counts=True)
-        got, gb, gt = lb.Traverser(bvh)(rays, counts=True)
-        assert_hits_equal(got, want)
-        assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
-    room = scenes.room_scene(seed=21)
-    prim = np.ascontiguousarray(scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))[::29])
-    want = port.trace(port.build(room, 16), room, prim, 16)
-    assert_hits_equal(lb.hits_view(lb.Traverser(lb.Builder(c)(dev(room)))(dev(prim))), want)
-    with pytest.raises(ValueError):
-        c.set_param(_lib.PARAM_TRACE_RAY_ORDER, 2)
