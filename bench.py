@@ -748,6 +748,8 @@ def main():
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
                     help="resident traversal CTAs per SM (default: the library's)")
+    ap.add_argument("--e2e-in-place", type=int, default=None,
+                    help="host rays / hits of the e2e step: 0 copied in chunks, 1 rays in place, 2 both in place")
     ap.add_argument("--trace-leaf-batch", type=int, default=None,
                     help="lanes with pending triangle tests before a traversal warp runs them (default: the library's)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
@@ -878,6 +880,8 @@ def main():
     bounce_pin = torch.from_numpy(bounce_h).pin_memory()
     out_p = torch.empty((prim.shape[0], 4), dtype=torch.float32).pin_memory()
     out_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32).pin_memory()
+    if args.e2e_in_place is not None:
+        ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, args.e2e_in_place)
     b_e2e = lb.BVH(ctx)
     for _ in range(2):
         tr = lb.Traverser(builder(tris_pin, into=b_e2e))
