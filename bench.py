@@ -750,6 +750,8 @@ def main():
                     help="resident traversal CTAs per SM (default: the library's)")
     ap.add_argument("--e2e-in-place", type=int, default=None,
                     help="host rays / hits of the e2e step: 0 copied in chunks, 1 rays in place, 2 both in place")
+    ap.add_argument("--e2e-chunk", type=int, default=None,
+                    help="rays per chunk of the e2e step's copied traces (0: one piece)")
     ap.add_argument("--trace-leaf-batch", type=int, default=None,
                     help="lanes with pending triangle tests before a traversal warp runs them (default: the library's)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-meshes measurement")
@@ -882,6 +884,8 @@ def main():
     out_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32).pin_memory()
     if args.e2e_in_place is not None:
         ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, args.e2e_in_place)
+    if args.e2e_chunk is not None:
+        ctx.set_param(_lib.PARAM_TRACE_CHUNK, args.e2e_chunk)
     b_e2e = lb.BVH(ctx)
     for _ in range(2):
         tr = lb.Traverser(builder(tris_pin, into=b_e2e))
@@ -915,6 +919,8 @@ def main():
     }
     detail("build_tuning", tuning)
     detail("trace_tuning", trace_tuning)
+    line["e2e"] = {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+                   "ms_per_step": round(e2e_ms, 4)}
     if args.only_step:
         line["gpu_launches"] = gpu_launches
         line["clocks"] = clk
