@@ -646,6 +646,16 @@ def measure_batched(ctx_device, steps, hbm_peak, peak_kind, n_meshes=4096, rays_
 # our arm
 
 
+TRANSFER_NOTE = {0: "triangles, rays and hits copied (page-locked host buffers)",
+                 1: "triangles copied; rays read in place in page-locked host memory, hits copied back",
+                 2: "triangles copied; rays read and hits written in place in page-locked host memory"}
+
+
+def ctx_in_place(ctx, transfer, args):
+    """The host-transfer mode the e2e steps ran with."""
+    return args.e2e_in_place if args.e2e_in_place is not None else transfer["trace_in_place"]
+
+
 def time_steps(builder, bvh, trav, tris, ray_sets, hit_sets, flush, stream, steps):
     """K whole steps (build, then one trace per ray set) timed with CUDA
     events on the launching stream, L2 flushed before each step. Returns
@@ -882,11 +892,16 @@ def main():
     bounce_pin = torch.from_numpy(bounce_h).pin_memory()
     out_p = torch.empty((prim.shape[0], 4), dtype=torch.float32).pin_memory()
     out_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32).pin_memory()
-    if args.e2e_in_place is not None:
-        ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, args.e2e_in_place)
     if args.e2e_chunk is not None:
         ctx.set_param(_lib.PARAM_TRACE_CHUNK, args.e2e_chunk)
     b_e2e = lb.BVH(ctx)
+    builder(tris_pin, into=b_e2e)
+    # how the host rays and hits travel (in place over the CPU-GPU link, or
+    # copied), tuned on these very buffers
+    transfer = autotune.tune_transfer(ctx, b_e2e, [(prim_pin, out_p), (bounce_pin, out_b)],
+                                      key=f"gb300:transfer:{WORKLOAD}")
+    if args.e2e_in_place is not None:
+        ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, args.e2e_in_place)
     for _ in range(2):
         tr = lb.Traverser(builder(tris_pin, into=b_e2e))
         tr(prim_pin, out=out_p)
@@ -920,7 +935,8 @@ def main():
     detail("build_tuning", tuning)
     detail("trace_tuning", trace_tuning)
     line["e2e"] = {"value": round(world * m / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
-                   "ms_per_step": round(e2e_ms, 4)}
+                   "ms_per_step": round(e2e_ms, 4), "trace_in_place": int(ctx_in_place(ctx, transfer, args))}
+    detail("transfer_tuning", transfer)
     if args.only_step:
         line["gpu_launches"] = gpu_launches
         line["clocks"] = clk
@@ -985,7 +1001,8 @@ def main():
                    "ms_per_step": round(e2e_ms, 4),
                    "h2d_bytes_per_step": int(tris_h.nbytes + prim_h.nbytes + bounce_h.nbytes),
                    "d2h_bytes_per_step": int(m * 16),
-                   "transfer": "triangles copied; rays read and hits written in place in page-locked host memory"}
+                   "trace_in_place": line["e2e"]["trace_in_place"],
+                   "transfer": TRANSFER_NOTE[line["e2e"]["trace_in_place"]]}
     line["gpu_launches"] = gpu_launches
     line["clocks"] = clk
     if rank == 0:

@@ -14,6 +14,8 @@ Tunes, on a caller-supplied sample workload:
     (LBVH_PARAM_TRACE_LEAF_BATCH) and the ray-refill threshold, timed on a
     sample of the workload's rays -- long rays through loose trees gain from
     batching the triangle tests of a warp's lanes, short rays lose;
+  * the handling of page-locked host rays and hits (tune_transfer,
+    LBVH_PARAM_TRACE_IN_PLACE), timed on the caller's own buffers;
   * the plain build (tune_build), per size class (primitive counts in
     [2^k, 2^(k+1))): the keys-only sort's tile (LBVH_PARAM_SORT_TILE_KEYS:
     1,024 or 4,096 keys), whether the bucket sort runs
@@ -55,6 +57,7 @@ _PARAMS = {
     "sort_tile_keys": "PARAM_SORT_TILE_KEYS",
     "bucket_sort_min": "PARAM_BUCKET_SORT_MIN",
     "bounds_blocks_per_sm": "PARAM_BOUNDS_BLOCKS_PER_SM",
+    "trace_in_place": "PARAM_TRACE_IN_PLACE",
 }
 
 
@@ -254,6 +257,46 @@ def tune_trace(ctx, bvh, rays, key: str, sample: int | None = None, reps: int = 
     setting = {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid,
                "sample_rays": int(part.shape[0]),
                "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in ms.items()}}
+    _store(table, key, setting, table_path)
+    apply(ctx, setting)
+    return setting
+
+
+TRACE_IN_PLACE = (0, 1, 2)
+
+
+def tune_transfer(ctx, bvh, pairs, key: str, reps: int = 2, table_path: str | None = None,
+                  force: bool = False) -> dict:
+    """Best handling of host rays and hits (LBVH_PARAM_TRACE_IN_PLACE: 0
+    copies both, 1 reads the rays in place and copies the hits back, 2 also
+    writes the hits in place) for tracing page-locked host ray arrays
+    against `bvh`: `pairs` is a list of (rays, hits) host arrays traced one
+    after the other, as the caller's step does. Long traces favour copying
+    the hits back once; short ones favour writing them in place. Cached
+    under `key`; returns the setting and applies it."""
+    import time
+
+    from .api import Traverser
+
+    table = load_table(table_path)
+    if key in table and not force:
+        apply(ctx, table[key])
+        return table[key]
+    trav = Traverser(bvh)
+    ms = {}
+    for mode in TRACE_IN_PLACE:
+        ctx.set_param(_lib.PARAM_TRACE_IN_PLACE, mode)
+        for r, h in pairs:  # first touch of this mode's paths
+            trav(r, out=h)
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            for r, h in pairs:
+                trav(r, out=h)  # host buffers: each call returns finished
+            ts.append(1e3 * (time.perf_counter() - t0))
+        ms[mode] = float(np.median(ts))
+    best = min(ms, key=ms.get)
+    setting = {"trace_in_place": best, "host_trace_ms": {str(k): round(v, 4) for k, v in ms.items()}}
     _store(table, key, setting, table_path)
     apply(ctx, setting)
     return setting
