@@ -142,15 +142,19 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
 #define LBVH_PARAM_BUCKET_SORT_MIN 12    /* keys-only builds of at least this many primitives sort by
                                             buckets of the top 12 code bits (>= 65,536; default 1,500,000) */
 #define LBVH_PARAM_BOUNDS_BLOCKS_PER_SM 13 /* CTAs per SM of the bounds pass, 1..16 (default 4) */
-#define LBVH_PARAM_TREE_WALK_FUSED 14    /* trees of more than 49,152 primitives: 0 (default) walks the
-                                            nodes crossing CTA edges in a separate kernel after the local
-                                            tree phase, 1 from each CTA's tail of that phase */
+#define LBVH_PARAM_TREE_WALK_FUSED 14    /* trees of more than 49,152 primitives: 0 (default) merges the
+                                            subtrees the local tree phase leaves at its CTA edges in
+                                            shared memory, window by window; 1 walks them up through
+                                            device-scope slots from each CTA's tail of the local phase */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */
 #define LBVH_PARAM_TEST_LOOKBACK_STALL 7 /* test only: 1 makes every look-back wait for a word no tile
                                             ever writes, so each wait runs out after the spin limit and
                                             the build reports LBVH_ERR_TIMEOUT; 0 (default) for real use */
+#define LBVH_PARAM_TEST_TREE_MERGE_CAP 15 /* test only: subtrees one tree-merge CTA holds in shared memory,
+                                            1..3200; fewer than a window has make the build take the
+                                            merge's fallback walk; 0 (default) for real use */
 LBVH_API int lbvh_ctx_set_param(lbvh_ctx* ctx, int param, int value);
 
 /* Replaces the reference triangle constructor triangle<float>(a, b, c)

@@ -218,7 +218,7 @@ ws_reserve(lbvh_ctx* c, size_t n)
   const size_t o_child = take(8 * n);
   const size_t o_lp = take(4 * n);
   const size_t o_np = take(4 * n);
-  const size_t o_pend = take(32 * size_t(kTreePendingPerBlock) * ((n + kTreeBlock - 1) / kTreeBlock));
+  const size_t o_pend = take(tree_scratch(n).bytes);
   const size_t o_boxes = take(24 * n);
   CK(reserve(c->ws, off, c->stream), "workspace allocation");
   // The look-back buffer only ever holds look-back words: fresh words read as
@@ -434,12 +434,12 @@ refit_common(lbvh_ctx* c, lbvh_bvh* bvh, const float* prims, int kind)
   if (bvh->codes_valid && n >= kRefitFromCodesMin) {
     // The build's sorted codes determine the topology: rerun its tree phase
     // (the same nodes, the same fit order) over the moved primitives. Its
-    // pending-node counter is reset here, as the bounds pass does in a build.
+    // merge-fallback flag is reset here, as the bounds pass does in a build.
     // (Measured: 0.59 against 1.19 ms at 16M triangles, 0.100 against 0.115
     // ms at 2^20; below 2^19 the walk over the links is the faster.)
     BuildBuffers b = c->bufs;
     b.keys_a = static_cast<uint32_t*>(bvh->codes.ptr);
-    CK(cudaMemsetAsync(&c->state->pending_count, 0, 4, c->stream), "state reset");
+    CK(cudaMemsetAsync(&c->state->tree_fallback, 0, 4, c->stream), "state reset");
     const Tri* tris = static_cast<const Tri*>(dprims);
     const Box* boxes = static_cast<const Box*>(dprims);
     if (bvh->flags & LBVH_BUILD_SORTED_LEAVES) {
@@ -699,6 +699,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
       if (value < 1 || value > (1 << 24))
         return fail(c, LBVH_ERR_INVALID_ARG, "look-back spin limit %d outside [1, 2^24]", value);
       c->bufs.spin_limit = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_TEST_TREE_MERGE_CAP:
+      if (value < 0 || value > int(kMergeCap))
+        return fail(c, LBVH_ERR_INVALID_ARG, "tree merge capacity %d outside [0, %u]", value, kMergeCap);
+      c->bufs.merge_cap = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_TEST_LOOKBACK_STALL:
       if (value < 0 || value > 1)

@@ -120,7 +120,7 @@ k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __res
       st->scale[k] = fdiv(1024.0f, fadd(fsub(r.v[k + 3], r.v[k]), 1.0f));
     }
     st->done_counter = 0;
-    st->pending_count = 0;
+    st->tree_fallback = 0;
     st->bucket_next = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++)
@@ -898,13 +898,14 @@ k_bucket_sort(const uint32_t* __restrict__ kin, uint32_t* __restrict__ kout, Bui
 // the CTA's edge (a "CTA root"). After a barrier, a slot holding a single
 // arrival marks a node whose sibling range leaves the CTA. Those nodes and the
 // CTA roots -- the canonical pieces of the CTA's slot range, at most two per
-// tree level -- go to a pending list; the CTA's finished records are written
-// out coalesced.
+// tree level, which together cover the range -- are written out in leaf
+// order; the CTA's finished records are written out coalesced.
 //
-// Global phase (k_tree_global), one thread per pending node, launched after
-// the local phase so that CTAs are not held by the long global chains: the
-// same walk over the global epoch-tagged slots. Every record a thread writes
-// is published by the release half of its next global arrival (an acq_rel exchange).
+// Merge phase (k_tree_merge, below): the nodes above the pieces, built window
+// by window in shared memory. (With LBVH_PARAM_TREE_WALK_FUSED the local
+// phase's own threads walk its pieces up through the global epoch-tagged
+// slots instead; every record such a thread writes is published by the
+// release half of its next global arrival, an acq_rel exchange.)
 
 struct PendingNode
 {
@@ -912,6 +913,22 @@ struct PendingNode
   Box box;
 };
 static_assert(sizeof(PendingNode) == 32, "pending record layout");
+
+// A piece record as two 16-byte stores / loads (records start on 32 bytes).
+__device__ __forceinline__ void
+store_piece(PieceRec* p, uint32_t R, int dR, const Box& b)
+{
+  float4* dst = reinterpret_cast<float4*>(p);
+  dst[0] = make_float4(__uint_as_float(R), __int_as_float(dR), b.lo[0], b.lo[1]);
+  dst[1] = make_float4(b.lo[2], b.hi[0], b.hi[1], b.hi[2]);
+}
+
+__device__ __forceinline__ Box
+load_piece_box(const PieceRec* p)
+{
+  const float4 a = __ldcg(reinterpret_cast<const float4*>(p)), c = __ldcg(reinterpret_cast<const float4*>(p) + 1);
+  return Box{ { a.z, a.w, c.x }, { c.y, c.z, c.w } };
+}
 
 constexpr uint32_t kSlotEmpty = 0xffffffffu;    // no arrival yet
 constexpr uint32_t kSlotComplete = 0xfffffffeu; // both children arrived
@@ -921,8 +938,9 @@ constexpr uint32_t kSlotComplete = 0xfffffffeu; // both children arrived
 // to arrive parks its far range end and stops, the second completes the
 // parent (its record is published by the release half of this thread's next
 // arrival) and climbs on. Node records the sibling's walk wrote are read
-// after the acquire half of this thread's arrival.
-template<class Leaf>
+// after the acquire half of this thread's arrival. kOneCta: every walk of
+// the tree runs in one CTA, so the arrivals are ordered at block scope.
+template<class Leaf, bool kOneCta = false>
 __device__ __forceinline__ void
 walk_global(const Leaf& leaf, uint32_t n, const uint32_t* __restrict__ codes, unsigned long long* __restrict__ slots,
             Node* __restrict__ nodes, BuildState* __restrict__ st, uint32_t epoch, uint32_t L, uint32_t R, Box box)
@@ -935,7 +953,8 @@ walk_global(const Leaf& leaf, uint32_t n, const uint32_t* __restrict__ codes, un
       return;
     }
     const uint32_t s = is_left ? R : L - 1;
-    const unsigned long long old = arrive_acq_rel(slots + s, tag | (is_left ? L : R));
+    const unsigned long long v = tag | (is_left ? L : R);
+    const unsigned long long old = kOneCta ? arrive_acq_rel_cta_global(slots + s, v) : arrive_acq_rel(slots + s, v);
     if (uint32_t(old >> 32) != epoch)
       return; // first arrival: the sibling completes the parent
     const uint32_t far = uint32_t(old);
@@ -966,8 +985,8 @@ k_tree_local(Leaf leaf,
              uint32_t n,
              const uint32_t* __restrict__ codes,
              Node* __restrict__ nodes,
-             PendingNode* __restrict__ pending_out,
-             uint32_t pending_cap,
+             PieceRec* __restrict__ pieces_out,
+             PieceHdr* __restrict__ hdr_out,
              BuildState* __restrict__ st,
              unsigned long long* __restrict__ slots,
              uint32_t epoch,
@@ -979,7 +998,7 @@ k_tree_local(Leaf leaf,
   uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_delta + kTreeBlock + 8);   // kTreeBlock
   Node* s_rec = reinterpret_cast<Node*>(s_slot + kTreeBlock);                 // kTreeBlock
   __shared__ PendingNode s_pend[kTreePendingPerBlock];
-  __shared__ uint32_t s_next, s_npend, s_base;
+  __shared__ uint32_t s_next, s_npend;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31;
   const uint32_t b0 = blockIdx.x * kTreeBlock;
@@ -1116,97 +1135,234 @@ k_tree_local(Leaf leaf,
     }
     return;
   }
+  // the CTA's pieces in leaf order, after its header, for the merge phase
+  const uint32_t m = min(np, kTreePendingPerBlock);
   if (tid == 0) {
     if (np > kTreePendingPerBlock)
       atomicOr(&st->error, kErrBadTopology); // more canonical pieces than a tree can have
-    s_base = np ? atomicAdd(&st->pending_count, min(np, kTreePendingPerBlock)) : 0;
+    hdr_out[blockIdx.x] = PieceHdr{ m, b0, s_delta[0], 0 };
   }
-  __syncthreads();
-  for (uint32_t k = tid; k < min(np, kTreePendingPerBlock); k += kTreeThreads) {
-    const uint32_t at = s_base + k;
-    if (at < pending_cap)
-      pending_out[at] = s_pend[k];
+  PieceRec* out = pieces_out + size_t(blockIdx.x) * kMergeOut;
+  for (uint32_t k = tid; k < m; k += kTreeThreads) {
+    const PendingNode pn = s_pend[k];
+    uint32_t rank = 0; // the pieces partition the CTA's range: their first leaves differ
+    for (uint32_t j = 0; j < m; j++)
+      rank += s_pend[j].L < pn.L;
+    store_piece(out + rank, pn.R, s_delta[pn.R - b0 + 1], pn.box);
+  }
+}
+
+// Merge phase: one CTA per window of `window` consecutive groups of the level
+// below. The window's P pieces are numbered in leaf order; boundary k lies
+// between pieces k and k + 1, at split position R_k. A node covering pieces
+// [a, b] is a left child, with its parent's split at boundary b, when
+// delta(R_b) > delta(L_a - 1), else a right child with the split at boundary
+// a - 1: the reference's rule over the same deltas, so these are the nodes a
+// walk from the leaves finds. An arrival stores its box in its side of the
+// boundary's box pair and swaps its far piece index into the boundary's slot
+// (block-scope acquire-release exchange on shared memory); the first arrival
+// stops, the second reads its sibling's box and far end, writes the parent's
+// record and climbs on, so each step of a chain is a few shared-memory round
+// trips. A walk stops at the window's edge (boundary -1 or P - 1); after a
+// barrier a slot still holding one arrival marks a node whose sibling leaves
+// the window. Those nodes are the window's pieces for the next level. The
+// last level is one window over everything and ends at the root.
+//
+// A window with more than `cap` pieces (kMergeCap: ~11 pieces come per
+// local-phase CTA, ~15-20 per window, so this is far from reached) sets
+// tree_fallback; the later levels see it and return, and the last one walks
+// every local-phase piece up through the global epoch-tagged slots instead
+// (walk_global at block scope), which holds for any number of pieces.
+struct MergeOut
+{
+  uint32_t L, R;
+  int32_t dR;
+  Box box;
+};
+
+// Largest g < ng with pre[g] <= i (pre[0] = 0 <= i < pre[ng]): the group of piece i.
+__device__ __forceinline__ uint32_t
+group_of(const uint32_t* pre, uint32_t ng, uint32_t i)
+{
+  uint32_t lo = 0, hi = ng;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (pre[mid] <= i)
+      lo = mid;
     else
-      atomicOr(&st->error, kErrBadTopology);
+      hi = mid;
   }
+  return lo;
 }
 
 template<class Leaf>
-__global__ __launch_bounds__(kFitThreads) void
-k_tree_global(Leaf leaf,
-              uint32_t n,
-              const uint32_t* __restrict__ codes,
-              unsigned long long* __restrict__ slots,
-              Node* __restrict__ nodes,
-              const PendingNode* __restrict__ pending_in,
-              BuildState* __restrict__ st,
-              uint32_t epoch)
+__global__ __launch_bounds__(kMergeThreads) void
+k_tree_merge(Leaf leaf,
+             uint32_t n,
+             const uint32_t* __restrict__ codes,
+             unsigned long long* __restrict__ slots,
+             uint32_t epoch,
+             Node* __restrict__ nodes,
+             BuildState* __restrict__ st,
+             const PieceRec* __restrict__ in,
+             const PieceHdr* __restrict__ in_hdr,
+             uint32_t groups,
+             uint32_t window,
+             PieceRec* __restrict__ out,
+             PieceHdr* __restrict__ out_hdr,
+             const PieceRec* __restrict__ first,
+             const PieceHdr* __restrict__ first_hdr,
+             uint32_t first_groups,
+             uint32_t cap,
+             bool last)
 {
   pdl_begin(); // the predecessor in the stream has finished
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= min(__ldg(&st->pending_count), uint32_t(gridDim.x * blockDim.x)))
-    return;
-  if (__ldcg(&st->error) & kErrLookbackTimeout)
-    return; // the sort gave up: no tree (the error is reported)
-  const PendingNode pn = pending_in[i];
-  // records from the local phase are visible at launch
-  walk_global(leaf, n, codes, slots, nodes, st, epoch, pn.L, pn.R, pn.box);
-}
+  extern __shared__ __align__(32) unsigned char smem[];
+  Box* s_box = reinterpret_cast<Box*>(smem);                                   // 2 x kMergeCap
+  uint32_t* s_R = reinterpret_cast<uint32_t*>(s_box + 2 * kMergeCap);          // kMergeCap
+  uint32_t* s_slot = s_R + kMergeCap;                                          // kMergeCap
+  uint32_t* s_pre = s_slot + kMergeCap;                                        // kMergeMaxGroups + 1
+  MergeOut* s_out = reinterpret_cast<MergeOut*>(s_pre + kMergeMaxGroups + 1);  // kMergeOut
+  int8_t* s_d = reinterpret_cast<int8_t*>(s_out + kMergeOut);                  // kMergeCap
+  __shared__ uint32_t s_nout, s_fallback;
 
-// The global phase for trees whose n - 1 split positions fit in shared
-// memory: one CTA walks every pending node, with its arrival slots in shared
-// memory and block-scope acquire-release arrivals (a chain of dependent
-// device-scope arrivals costs about a microsecond per tree level; these cost
-// a fraction of that). Records still go to the node array: a record is
-// published by the release half of its writer's next arrival and read after
-// the acquire half of the sibling's, both at block scope.
-template<class Leaf>
-__global__ __launch_bounds__(kTreeGlobalCtaThreads) void
-k_tree_global_cta(Leaf leaf,
-                  uint32_t n,
-                  const uint32_t* __restrict__ codes,
-                  Node* __restrict__ nodes,
-                  const PendingNode* __restrict__ pending_in,
-                  uint32_t pending_cap,
-                  BuildState* __restrict__ st)
-{
-  pdl_begin(); // the predecessor in the stream has finished
-  extern __shared__ uint32_t s_slots[]; // n - 1 split positions
   if (__ldcg(&st->error) & kErrLookbackTimeout)
     return; // the sort gave up: no tree (the error is reported); uniform over the CTA
-  for (uint32_t j = threadIdx.x; j + 1 < n; j += blockDim.x)
-    s_slots[j] = kSlotEmpty;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t g0 = blockIdx.x * window, ng = min(window, groups - g0);
+  if (tid == 0) {
+    s_nout = 0;
+    s_fallback = __ldcg(&st->tree_fallback); // set by an earlier level only
+    s_pre[0] = 0;
+  }
+  for (uint32_t g = tid; g < ng; g += kMergeThreads)
+    s_pre[g + 1] = min(__ldcg(&in_hdr[g0 + g].count), kMergeOut);
   __syncthreads();
-  const uint32_t count = min(__ldcg(&st->pending_count), pending_cap);
-  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
-    const PendingNode pn = pending_in[i];
-    uint32_t L = pn.L, R = pn.R;
-    Box box = pn.box;
-    bool is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
+  if (tid < 32) { // running sum of the group counts
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < ng; base += 32) {
+      const uint32_t g = base + tid;
+      uint32_t v = g < ng ? s_pre[g + 1] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (int(tid) >= o)
+          v += t;
+      }
+      if (g < ng)
+        s_pre[g + 1] = v + carry;
+      carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+  }
+  __syncthreads();
+  const uint32_t P = s_pre[ng];
+  const uint32_t L0 = __ldcg(&in_hdr[g0].L0);
+  const int dL0 = __ldcg(&in_hdr[g0].dL);
+
+  if (s_fallback || P > cap) { // uniform over the CTA
+    if (!last) {
+      if (tid == 0)
+        atomicExch(&st->tree_fallback, 1u);
+      return;
+    }
+    for (size_t idx = tid; idx < size_t(first_groups) * kMergeOut; idx += kMergeThreads) {
+      const uint32_t c = uint32_t(idx / kMergeOut), k = uint32_t(idx % kMergeOut);
+      if (k >= min(__ldcg(&first_hdr[c].count), kMergeOut))
+        continue;
+      const PieceRec* p = first + idx;
+      const uint32_t L = k == 0 ? __ldcg(&first_hdr[c].L0) : __ldcg(&p[-1].R) + 1;
+      walk_global<Leaf, true>(leaf, n, codes, slots, nodes, st, epoch, L, __ldcg(&p->R), load_piece_box(p));
+    }
+    return;
+  }
+
+  for (uint32_t i = tid; i < P; i += kMergeThreads) {
+    const uint32_t g = group_of(s_pre, ng, i);
+    const PieceRec* p = in + size_t(g0 + g) * kMergeOut + (i - s_pre[g]);
+    s_R[i] = __ldcg(&p->R);
+    s_d[i] = int8_t(__ldcg(&p->dR));
+    s_slot[i] = kSlotEmpty;
+  }
+  __syncthreads();
+
+  for (uint32_t i = tid; i < P; i += kMergeThreads) {
+    const uint32_t g = group_of(s_pre, ng, i);
+    Box box = load_piece_box(in + size_t(g0 + g) * kMergeOut + (i - s_pre[g]));
+    uint32_t a = i, b = i;
+    uint32_t L = i == 0 ? L0 : s_R[i - 1] + 1, R = s_R[i];
+    int dl = i == 0 ? dL0 : s_d[i - 1], dr = s_d[i];
     for (uint32_t depth = 0;; depth++) {
       if (depth > kMaxTreeDepth + 2) {
         atomicOr(&st->error, kErrBadTopology);
         break;
       }
-      const uint32_t s = is_left ? R : L - 1;
-      const uint32_t old = arrive_acq_rel_cta(s_slots + s, is_left ? L : R);
+      const bool is_left = dr > dl; // delta(R) > delta(L - 1)
+      if (is_left ? b + 1 >= P : a == 0) { // the parent's split is on the window's edge
+        const uint32_t j = atomicAdd(&s_nout, 1u);
+        if (j < kMergeOut)
+          s_out[j] = MergeOut{ L, R, dr, box };
+        break;
+      }
+      const uint32_t k = is_left ? b : a - 1;
+      s_box[2 * k + (is_left ? 0 : 1)] = box;
+      // release publishes this box, acquire makes the sibling's visible
+      const uint32_t old = arrive_acq_rel_cta(s_slot + k, is_left ? a : b);
       if (old == kSlotEmpty)
         break; // first arrival: the sibling completes the parent
-      const uint32_t LP = is_left ? L : old, RP = is_left ? old : R;
+      s_slot[k] = kSlotComplete; // read only after the barrier below
+      const Box other = s_box[2 * k + (is_left ? 1 : 0)];
+      box = is_left ? join(box, other) : join(other, box);
+      if (is_left)
+        b = old;
+      else
+        a = old;
+      const uint32_t s = s_R[k];
+      const uint32_t LP = a == 0 ? L0 : s_R[a - 1] + 1, RP = s_R[b];
       const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
       const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
-      const uint32_t sib = is_left ? cr : cl;
-      const Box other = (sib & kLeafBit) ? leaf(sib & ~kLeafBit) : load_node_box(nodes, sib);
-      box = is_left ? join(box, other) : join(other, box);
       L = LP;
       R = RP;
+      dl = a == 0 ? dL0 : s_d[a - 1];
+      dr = s_d[b];
       if (L == 0 && R == n - 1) {
         store_node(nodes, 0, box, cl, cr);
         break;
       }
-      is_left = boundary_delta(codes, n, R) > boundary_delta(codes, n, L - 1);
-      store_node(nodes, is_left ? R : L, box, cl, cr);
+      store_node(nodes, dr > dl ? R : L, box, cl, cr);
     }
+  }
+  __syncthreads();
+
+  // single arrivals: nodes whose sibling range leaves the window
+  for (uint32_t k = tid; k + 1 < P; k += kMergeThreads) {
+    const uint32_t v = s_slot[k];
+    if (v == kSlotEmpty || v == kSlotComplete)
+      continue;
+    const bool left = v <= k; // the waiter covers pieces [v, k] (a left child) or [k + 1, v]
+    const uint32_t a = left ? v : k + 1, b = left ? k : v;
+    const uint32_t j = atomicAdd(&s_nout, 1u);
+    if (j < kMergeOut)
+      s_out[j] = MergeOut{ a == 0 ? L0 : s_R[a - 1] + 1, s_R[b], s_d[b], s_box[2 * k + (left ? 0 : 1)] };
+  }
+  __syncthreads();
+  const uint32_t nout = s_nout;
+  if (last) {
+    if (tid == 0 && nout != 0)
+      atomicOr(&st->error, kErrBadTopology); // the root was not reached
+    return;
+  }
+  const uint32_t m = min(nout, kMergeOut);
+  if (tid == 0) {
+    if (nout > kMergeOut)
+      atomicOr(&st->error, kErrBadTopology); // more canonical pieces than a tree can have
+    out_hdr[blockIdx.x] = PieceHdr{ m, L0, dL0, 0 };
+  }
+  for (uint32_t k = tid; k < m; k += kMergeThreads) {
+    const MergeOut o = s_out[k];
+    uint32_t rank = 0;
+    for (uint32_t j = 0; j < m; j++)
+      rank += s_out[j].L < o.L;
+    store_piece(out + size_t(blockIdx.x) * kMergeOut + rank, o.R, o.dR, o.box);
   }
 }
 
@@ -1472,28 +1628,30 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
   if (!(configured.load(std::memory_order_relaxed) & bit)) {
     e = cudaFuncSetAttribute(k_tree_local<Leaf>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTreeSmem));
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_tree_global_cta<Leaf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               int(4 * kTreeGlobalCtaMaxPrims));
+      e = cudaFuncSetAttribute(k_tree_merge<Leaf>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kMergeSmem));
     if (e != cudaSuccess)
       return e;
     configured.fetch_or(bit, std::memory_order_relaxed);
   }
   const uint32_t blocks = ceil_div_u32(n, kTreeBlock);
-  const uint32_t cap = blocks * kTreePendingPerBlock;
-  // trees beyond the one-CTA global phase walk their CTA edges in a
-  // separate kernel, or (when the context asks) from the local phase's tail
+  const TreeScratch ts = tree_scratch(n);
+  char* pend = static_cast<char*>(b.pending);
+  auto pieces = [&](uint32_t lv) { return reinterpret_cast<PieceRec*>(pend + ts.pieces[lv]); };
+  auto hdrs = [&](uint32_t lv) { return reinterpret_cast<PieceHdr*>(pend + ts.hdrs[lv]); };
+  // trees beyond the fused-walk threshold walk their CTA edges from the local
+  // phase's tail when the context asks; all others merge the local pieces
   const bool walk_on = blocks > 1 && n > kTreeGlobalCtaMaxPrims && b.walk_fused == 1;
-  CUDA_TRY(launch_pdl(k_tree_local<Leaf>, blocks, kTreeThreads, kTreeSmem, s, leaf, n, b.keys_a, nodes,
-                      reinterpret_cast<PendingNode*>(b.pending), cap, b.state, b.slots, epoch, walk_on));
+  CUDA_TRY(launch_pdl(k_tree_local<Leaf>, blocks, kTreeThreads, kTreeSmem, s, leaf, n, b.keys_a, nodes, pieces(0),
+                      hdrs(0), b.state, b.slots, epoch, walk_on));
   if (blocks == 1 || walk_on)
     return cudaGetLastError(); // the whole tree was built in the one CTA, or by the walks
-  if (n <= kTreeGlobalCtaMaxPrims) {
-    CUDA_TRY(launch_pdl(k_tree_global_cta<Leaf>, 1, kTreeGlobalCtaThreads, size_t(4) * (n - 1), s, leaf, n, b.keys_a,
-                        nodes, reinterpret_cast<const PendingNode*>(b.pending), cap, b.state));
-    return cudaGetLastError();
+  const uint32_t cap = (b.merge_cap && b.merge_cap < kMergeCap) ? b.merge_cap : kMergeCap;
+  for (uint32_t lv = 0; lv < ts.merges; lv++) {
+    const bool last = lv + 1 == ts.merges;
+    CUDA_TRY(launch_pdl(k_tree_merge<Leaf>, ceil_div_u32(ts.groups[lv], ts.window[lv]), kMergeThreads, kMergeSmem, s,
+                        leaf, n, b.keys_a, b.slots, epoch, nodes, b.state, pieces(lv), hdrs(lv), ts.groups[lv],
+                        ts.window[lv], pieces(lv + 1), hdrs(lv + 1), pieces(0), hdrs(0), ts.groups[0], cap, last));
   }
-  CUDA_TRY(launch_pdl(k_tree_global<Leaf>, ceil_div_u32(cap, kFitThreads), kFitThreads, 0, s, leaf, n, b.keys_a,
-                      b.slots, nodes, reinterpret_cast<const PendingNode*>(b.pending), b.state, epoch));
   return cudaGetLastError();
 }
 

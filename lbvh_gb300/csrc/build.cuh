@@ -54,15 +54,92 @@ constexpr uint32_t kTreeThreads = 256; // threads per CTA of the tree build (4 s
 // dynamic shared memory of the tree build: deltas, slots, node records (each
 // array starts on a 32-byte boundary)
 constexpr size_t kTreeSmem = (kTreeBlock + 8) * 4 + kTreeBlock * 4 + kTreeBlock * 32;
-// Trees of up to this many primitives finish their global phase in one CTA
-// with the arrival slots in shared memory (4 bytes per split position).
+// Trees beyond this many primitives may walk their CTA-edge nodes from the
+// local phase's tail (LBVH_PARAM_TREE_WALK_FUSED).
 constexpr uint32_t kTreeGlobalCtaMaxPrims = 49152;
-constexpr int kTreeGlobalCtaThreads = 1024;
 static_assert(((kTreeBlock + 8) * 4) % 32 == 0 && (kTreeBlock * 4) % 32 == 0, "smem alignment");
 constexpr uint32_t kSpinLimit = 1u << 22;   // look-back polls before giving up
 constexpr int kLookbackWindow = 8;          // look-back words read per poll
 constexpr uint32_t kMaxTreeDepth = 64;      // 30-bit codes + 32-bit index tie-break
 constexpr uint32_t kMaxPrims = (1u << 30) - 1; // look-back counts are 30-bit
+
+// Merge phase of the tree build (k_tree_merge). The local phase leaves, per
+// CTA, the maximal subtrees it completed -- its "pieces", which partition the
+// CTA's leaf range -- ordered by first leaf, after a header. One merge CTA
+// takes a window of consecutive groups (CTAs of the local phase, or windows
+// of the level below), builds the nodes above their pieces with every
+// arrival slot and child box in shared memory, and leaves the pieces of its
+// window the same way; the last level is one CTA that reaches the root.
+struct PieceRec
+{
+  uint32_t R;  // last leaf of the piece (its first is the previous piece's R + 1)
+  int32_t dR;  // boundary delta after the piece: delta(R)
+  Box box;
+};
+static_assert(sizeof(PieceRec) == 32, "piece record layout");
+struct PieceHdr
+{
+  uint32_t count; // pieces of the group
+  uint32_t L0;    // first leaf of the group
+  int32_t dL;     // boundary delta before the group: delta(L0 - 1)
+  uint32_t pad;
+};
+static_assert(sizeof(PieceHdr) == 16, "piece header layout");
+constexpr int kMergeThreads = 1024;
+constexpr uint32_t kMergeCap = 3200;        // pieces a merge CTA holds in shared memory
+constexpr uint32_t kMergeGroups = 128;      // groups per window below the last level
+constexpr uint32_t kMergeFinalFirst = 160;  // local-phase groups the last level takes at once
+constexpr uint32_t kMergeFinalLater = 96;   // window groups the last level takes at once
+constexpr uint32_t kMergeMaxGroups = 160;   // largest window
+constexpr uint32_t kMergeMaxLevels = 4;     // 2^30 leaves: 2^20 CTAs -> 8192 -> 64 -> 1
+constexpr uint32_t kMergeOut = kTreePendingPerBlock; // pieces a window leaves (two per tree level)
+// shared memory of k_tree_merge: group prefix, piece ends, deltas, slots,
+// two child boxes per slot, the window's own pieces
+constexpr size_t kMergeSmem = size_t(kMergeMaxGroups + 1) * 4 + size_t(kMergeCap) * (4 + 4 + 1) +
+                              size_t(kMergeCap) * 2 * sizeof(Box) + size_t(kMergeOut) * 48 + 64;
+
+constexpr size_t
+align256(size_t x)
+{
+  return (x + 255) / 256 * 256;
+}
+
+// Where each level's pieces and headers live in the build's pending area:
+// level 0 is written by the local phase (one group per CTA), level k >= 1 by
+// the k-th merge launch (one group per window); the last launch writes none.
+struct TreeScratch
+{
+  uint32_t merges;                          // merge launches (0: the local phase built the whole tree)
+  uint32_t groups[kMergeMaxLevels + 1];     // groups of each level
+  uint32_t window[kMergeMaxLevels];         // groups per window of each merge launch
+  size_t pieces[kMergeMaxLevels + 1];       // byte offsets
+  size_t hdrs[kMergeMaxLevels + 1];
+  size_t bytes;
+};
+
+constexpr TreeScratch
+tree_scratch(size_t n)
+{
+  TreeScratch t{};
+  uint32_t g = uint32_t((n + kTreeBlock - 1) / kTreeBlock);
+  size_t off = 0;
+  for (uint32_t lv = 0;; lv++) {
+    t.groups[lv] = g;
+    t.pieces[lv] = off;
+    off = align256(off + size_t(g) * kMergeOut * sizeof(PieceRec));
+    t.hdrs[lv] = off;
+    off = align256(off + size_t(g) * sizeof(PieceHdr));
+    if (g <= 1 || lv == kMergeMaxLevels)
+      break;
+    const uint32_t final_max = lv == 0 ? kMergeFinalFirst : kMergeFinalLater;
+    const uint32_t w = g <= final_max ? g : kMergeGroups;
+    t.window[lv] = w;
+    t.merges = lv + 1;
+    g = (g + w - 1) / w;
+  }
+  t.bytes = off;
+  return t;
+}
 
 // Per-leaf box sources for the templated build kernels.
 struct TriLeaf
@@ -96,7 +173,7 @@ struct BuildBuffers
   uint32_t* leaf_parent;          // refit: n
   uint32_t* node_parent;          // refit: n-1
   unsigned long long* slots;      // n-1 epoch-tagged arrival slots (persistent)
-  void* pending;                  // tree build: 32 B x kTreePendingPerBlock per CTA
+  void* pending;                  // tree build: pieces and headers of every level (tree_scratch)
   Box* boxes;                     // optional: leaf boxes staged by the bounds pass (n)
   uint32_t bounds_blocks;
   uint32_t morton_blocks;
@@ -108,8 +185,10 @@ struct BuildBuffers
   uint32_t* top_rows;             // bucket sort: msd_ranges x kTopBuckets counts (in vals_a)
   uint32_t tile_keys;             // keys-only onesweep tile: 0 automatic (kSmallTile up to
                                   // kSmallTileMaxPrims codes, else kSortTile), or kSmallTile / kSortTile
-  uint32_t walk_fused;            // trees beyond kTreeGlobalCtaMaxPrims: 0 walk the nodes crossing CTA
-                                  // edges in a separate global kernel, 1 from the local phase's tail
+  uint32_t walk_fused;            // trees beyond kTreeGlobalCtaMaxPrims: 0 merge the local phase's
+                                  // pieces in shared memory, 1 walk them from the local phase's tail
+  uint32_t merge_cap;             // test only: pieces a merge CTA holds (0: kMergeCap); fewer make
+                                  // the merge fall back to its walk over global slots
   uint32_t spin_limit;            // look-back polls before a wait gives up (0: kSpinLimit)
   uint32_t wait_xor;              // test only: nonzero makes every look-back wait for a tag no
                                   // tile publishes, so each wait runs out (0 in normal use)

@@ -57,7 +57,7 @@ struct BuildState
   uint32_t hist[4][256];       // radix digit histograms of the Morton codes
   uint32_t tile_counter[4];    // onesweep tile id dispensers, one per pass
   uint32_t done_counter;       // last-block detection in the bounds kernel
-  uint32_t pending_count;      // tree build: nodes left for the global phase
+  uint32_t tree_fallback;      // tree build: a merge window overflowed; the last level walks instead
   uint32_t error;              // sticky kErr* bits
   uint32_t pad1;
   // keys-only sort by buckets of the top 12 code bits (see k_top_scan)

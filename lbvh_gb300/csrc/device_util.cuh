@@ -133,6 +133,16 @@ arrive_acq_rel(unsigned long long* slot, unsigned long long v)
   return old;
 }
 
+// The same arrival on a global slot, ordered at block scope: for walks
+// whose every arrival comes from threads of one CTA.
+__device__ __forceinline__ unsigned long long
+arrive_acq_rel_cta_global(unsigned long long* slot, unsigned long long v)
+{
+  unsigned long long old;
+  asm volatile("atom.acq_rel.cta.global.exch.b64 %0, [%1], %2;" : "=l"(old) : "l"(slot), "l"(v) : "memory");
+  return old;
+}
+
 // The same arrival on a shared-memory slot, ordered at block scope.
 __device__ __forceinline__ uint32_t
 arrive_acq_rel_cta(uint32_t* slot, uint32_t v)

@@ -55,9 +55,8 @@ constexpr size_t kOffKeysA = kOffPartials + round_up(kBoundsBlocksMax * 48);
 constexpr size_t kOffKeysB = kOffKeysA + round_up(4 * kNoAllocMaxPrims);
 constexpr size_t kOffLookback = kOffKeysB + round_up(4 * kNoAllocMaxPrims);
 constexpr size_t kOffSlots = kOffLookback + round_up(kTiles * 256 * 8);
-constexpr size_t kTreeBlocks = (kNoAllocMaxPrims + kTreeBlock - 1) / kTreeBlock;
 constexpr size_t kOffPending = kOffSlots + round_up(8 * kNoAllocMaxPrims);
-constexpr size_t kScratchBytes = kOffPending + round_up(32 * kTreePendingPerBlock * kTreeBlocks);
+constexpr size_t kScratchBytes = kOffPending + round_up(tree_scratch(kNoAllocMaxPrims).bytes);
 
 // The scratch memory of every allocation-free build on this device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];

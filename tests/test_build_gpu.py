@@ -204,16 +204,19 @@ def test_sort_and_bounds_parameters(lib_built, port, tile, bucket_min, bounds):
             c.set_param(param, bad)
 
 
-@pytest.mark.parametrize("fused", [0, 1])
-def test_tree_global_phase_fused_or_separate(lib_built, port, fused):
-    """The nodes crossing CTA edges, walked from the local phase's tail or
-    by a separate kernel afterwards, give the reference's nodes (and so do
-    builds small enough for the one-CTA global phase), for builds and for
+@pytest.mark.parametrize("fused,merge_cap", [(0, 0), (1, 0), (0, 8)])
+def test_tree_global_phase_fused_or_separate(lib_built, port, fused, merge_cap):
+    """The nodes above the subtrees the local phase leaves at its CTA edges
+    -- merged window by window in shared memory (one level up to 160 CTAs,
+    two beyond), walked from the local phase's tail, or (a merge capacity of
+    8 subtrees, too small for any window here) by the merge's fallback walk
+    over the global slots -- are the reference's nodes, for builds and for
     refits that rerun the tree phase over the build's codes."""
     from lbvh_gb300 import _lib
 
     c = lb.Context()
     c.set_param(_lib.PARAM_TREE_WALK_FUSED, fused)
+    c.set_param(_lib.PARAM_TEST_TREE_MERGE_CAP, merge_cap)
     for n in (20_000, 49_153, 300_007):
         t = scenes.soup(n, 70 + n % 5)
         assert nodes_equal(lb.Builder(c)(dev(t)).nodes(), port.build(t, 16)), (fused, n)
@@ -226,6 +229,8 @@ def test_tree_global_phase_fused_or_separate(lib_built, port, fused):
     assert nodes_equal(b.nodes(), port.refit(port.build(t, 16), t2))
     with pytest.raises(ValueError):
         c.set_param(_lib.PARAM_TREE_WALK_FUSED, 2)
+    with pytest.raises(ValueError):
+        c.set_param(_lib.PARAM_TEST_TREE_MERGE_CAP, 3201)
 
 
 def test_full_size_16m_build_parity(ctx, port):
