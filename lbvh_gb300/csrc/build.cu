@@ -1161,18 +1161,25 @@ k_tree_local(Leaf leaf,
 // walk from the leaves finds. An arrival stores its box in its side of the
 // boundary's box pair and swaps its far piece index into the boundary's slot
 // (block-scope acquire-release exchange on shared memory); the first arrival
-// stops, the second reads its sibling's box and far end, writes the parent's
-// record and climbs on, so each step of a chain is a few shared-memory round
-// trips. A walk stops at the window's edge (boundary -1 or P - 1); after a
-// barrier a slot still holding one arrival marks a node whose sibling leaves
-// the window. Those nodes are the window's pieces for the next level. The
-// last level is one window over everything and ends at the root.
+// stops, the second reads its sibling's box and far end, marks the slot
+// complete with the parent's piece range and climbs on, so each step of a
+// chain is a few shared-memory round trips. (No record is stored to global
+// memory during a walk: the release half of the next exchange would wait for
+// it.) A walk stops at the window's edge (boundary -1 or P - 1). After a
+// barrier every complete slot yields its node's record -- the two child boxes
+// are still in the pair, joined left then right -- and a slot still holding
+// one arrival marks a node whose sibling leaves the window. Those nodes are
+// the window's pieces for the next level. The last level is one window over
+// everything and ends at the root.
 //
 // A window with more than `cap` pieces (kMergeCap: ~11 pieces come per
 // local-phase CTA, ~15-20 per window, so this is far from reached) sets
 // tree_fallback; the later levels see it and return, and the last one walks
 // every local-phase piece up through the global epoch-tagged slots instead
 // (walk_global at block scope), which holds for any number of pieces.
+constexpr uint32_t kMergeDone = 0x80000000u; // slot: both arrived; bits 30-16 / 15-0 the parent's pieces
+static_assert(kMergeCap <= 0x7fffu, "piece indices of a complete slot take 15 bits");
+
 struct MergeOut
 {
   uint32_t L, R;
@@ -1278,9 +1285,9 @@ k_tree_merge(Leaf leaf,
 
   for (uint32_t i = tid; i < P; i += kMergeThreads) {
     const uint32_t g = group_of(s_pre, ng, i);
-    const PieceRec* p = in + size_t(g0 + g) * kMergeOut + (i - s_pre[g]);
-    s_R[i] = __ldcg(&p->R);
-    s_d[i] = int8_t(__ldcg(&p->dR));
+    const uint2 rd = __ldcg(reinterpret_cast<const uint2*>(in + size_t(g0 + g) * kMergeOut + (i - s_pre[g])));
+    s_R[i] = rd.x;
+    s_d[i] = int8_t(int(rd.y));
     s_slot[i] = kSlotEmpty;
   }
   __syncthreads();
@@ -1309,35 +1316,38 @@ k_tree_merge(Leaf leaf,
       const uint32_t old = arrive_acq_rel_cta(s_slot + k, is_left ? a : b);
       if (old == kSlotEmpty)
         break; // first arrival: the sibling completes the parent
-      s_slot[k] = kSlotComplete; // read only after the barrier below
       const Box other = s_box[2 * k + (is_left ? 1 : 0)];
       box = is_left ? join(box, other) : join(other, box);
       if (is_left)
         b = old;
       else
         a = old;
-      const uint32_t s = s_R[k];
-      const uint32_t LP = a == 0 ? L0 : s_R[a - 1] + 1, RP = s_R[b];
-      const uint32_t cl = (LP == s) ? (s | kLeafBit) : s;
-      const uint32_t cr = (RP == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
-      L = LP;
-      R = RP;
+      s_slot[k] = kMergeDone | (a << 16) | b; // read only after the barrier below
+      L = a == 0 ? L0 : s_R[a - 1] + 1;
+      R = s_R[b];
+      if (L == 0 && R == n - 1)
+        break; // the root
       dl = a == 0 ? dL0 : s_d[a - 1];
       dr = s_d[b];
-      if (L == 0 && R == n - 1) {
-        store_node(nodes, 0, box, cl, cr);
-        break;
-      }
-      store_node(nodes, dr > dl ? R : L, box, cl, cr);
     }
   }
   __syncthreads();
 
-  // single arrivals: nodes whose sibling range leaves the window
   for (uint32_t k = tid; k + 1 < P; k += kMergeThreads) {
     const uint32_t v = s_slot[k];
-    if (v == kSlotEmpty || v == kSlotComplete)
+    if (v == kSlotEmpty)
       continue;
+    if (v & kMergeDone) { // the record of the node completed here
+      const uint32_t a = (v >> 16) & 0x7fffu, b = v & 0xffffu, s = s_R[k];
+      const uint32_t L = a == 0 ? L0 : s_R[a - 1] + 1, R = s_R[b];
+      const uint32_t cl = (L == s) ? (s | kLeafBit) : s;
+      const uint32_t cr = (R == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
+      const int dl = a == 0 ? dL0 : s_d[a - 1];
+      const uint32_t idx = (L == 0 && R == n - 1) ? 0 : (s_d[b] > dl ? R : L);
+      store_node(nodes, idx, join(s_box[2 * k], s_box[2 * k + 1]), cl, cr);
+      continue;
+    }
+    // a single arrival: a node whose sibling range leaves the window
     const bool left = v <= k; // the waiter covers pieces [v, k] (a left child) or [k + 1, v]
     const uint32_t a = left ? v : k + 1, b = left ? k : v;
     const uint32_t j = atomicAdd(&s_nout, 1u);
