@@ -754,6 +754,8 @@ def main():
     ap.add_argument("--only-config1", action="store_true", help="only the mid-size torus step (profiling)")
     ap.add_argument("--tree-walk-fused", type=int, default=None,
                     help="1: walk tree nodes crossing CTA edges from the local phase's tail (default: the library's)")
+    ap.add_argument("--small-build-max", type=int, default=None,
+                    help="largest build run as one cluster launch, 0 = never (default: the library's)")
     ap.add_argument("--trace-refill", type=int, default=None,
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
@@ -802,6 +804,8 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
     if args.tree_walk_fused is not None:
         ctx.set_param(_lib.PARAM_TREE_WALK_FUSED, args.tree_walk_fused)
+    if args.small_build_max is not None:
+        ctx.set_param(_lib.PARAM_SMALL_BUILD_MAX, args.small_build_max)
 
     def detail(name, rec):
         if rank == 0:

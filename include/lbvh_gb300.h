@@ -146,6 +146,11 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             subtrees the local tree phase leaves at its CTA edges in
                                             shared memory, window by window; 1 walks them up through
                                             device-scope slots from each CTA's tail of the local phase */
+#define LBVH_PARAM_SMALL_BUILD_MAX 16   /* builds of up to this many primitives (0..16384, default 16384)
+                                            without LBVH_BUILD_SORTED_LEAVES or LBVH_BUILD_KEEP_CURVE run
+                                            as one launch: a cluster of up to 16 CTAs that keeps the
+                                            boxes, codes, sort and tree in shared memory; 0 always takes
+                                            the multi-kernel build (the same nodes either way) */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

@@ -64,6 +64,7 @@ struct lbvh_ctx
   uint32_t msd_min = kMsdMinPrims; // keys-only builds from this size use the bucket sort
   uint32_t bounds_per_sm = 4;      // bounds-pass CTAs per SM
   uint32_t walk_fused = 0;         // 1: CTA-edge walks from the local tree phase's tail, 0: separate kernel
+  uint32_t small_max = kSmallMaxPrims; // keys-only builds up to this size run as one cluster launch
   DevBuf batch_ws;                 // batched build: codes, boxes, slots
   uint32_t epoch = 0;          // look-back epoch of the last sort pass
   char msg[512] = { 0 };
@@ -298,6 +299,9 @@ set_device(lbvh_ctx* c)
 // build's sorted codes; smaller ones walk the node links.
 constexpr uint32_t kRefitFromCodesMin = 1u << 19;
 
+int build_multi(lbvh_ctx* c, BuildBuffers& b, const void* dprims, uint32_t nn, uint32_t flags, lbvh_bvh* bvh,
+                int kind, Node* nodes);
+
 // Shared build body for triangles and boxes.
 int
 build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh* bvh, int kind)
@@ -354,6 +358,41 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
     b.top_rows = b.vals_a;
   }
 
+  Node* nodes = static_cast<Node*>(bvh->nodes.ptr);
+  const bool small = !keep && !sorted_leaves && nn <= c->small_max && nn <= small_build_limit();
+  if (small) { // the whole build in one cluster launch
+    if (kind == kKindTris)
+      CK(launch_small_build_tris(static_cast<const Tri*>(dprims), nn, b.keys_a, nodes, c->state, c->stream),
+         "build launch");
+    else
+      CK(launch_small_build_boxes(static_cast<const Box*>(dprims), nn, b.keys_a, nodes, c->state, c->stream),
+         "build launch");
+  } else {
+    if ((st = build_multi(c, b, dprims, nn, flags, bvh, kind, nodes)))
+      return st;
+  }
+  bvh->n = nn;
+  bvh->flags = flags;
+  bvh->kind = kind;
+  bvh->wnodes_valid = false;
+  bvh->codes_valid = true;
+  bvh->prims = dprims;
+  bvh->device = c->device;
+  if (!on_device(prims))
+    return check_device(c); // host caller: finish and report before returning
+  return LBVH_OK;
+}
+
+// The multi-kernel build: bounds + codes, the sort, the tree phases.
+int
+build_multi(lbvh_ctx* c, BuildBuffers& b, const void* dprims, uint32_t nn, uint32_t flags, lbvh_bvh* bvh, int kind,
+            Node* nodes)
+{
+  int st = LBVH_OK;
+  const size_t n = nn;
+  const size_t rec = (kind == kKindTris) ? sizeof(Tri) : sizeof(Box);
+  const bool keep = flags & LBVH_BUILD_KEEP_CURVE;
+  const bool sorted_leaves = flags & LBVH_BUILD_SORTED_LEAVES;
   if (kind == kKindTris)
     CK(launch_curve_tris(static_cast<const Tri*>(dprims), nn, b, c->stream), "curve launch");
   else
@@ -374,7 +413,6 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
     CK(cudaMemcpyAsync(curve + n, b.keys_a, 4 * n, cudaMemcpyDeviceToDevice, c->stream), "curve copy");
     CK(cudaMemcpyAsync(curve + 2 * n, b.vals_a, 4 * n, cudaMemcpyDeviceToDevice, c->stream), "curve copy");
   }
-  Node* nodes = static_cast<Node*>(bvh->nodes.ptr);
   if (sorted_leaves) {
     CK(reserve(bvh->sorted_prims, rec * n, c->stream), "sorted primitive allocation");
     CK(reserve(bvh->leaf_prim, 4 * n, c->stream), "leaf map allocation");
@@ -394,16 +432,7 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
     else
       CK(launch_fit_boxes(static_cast<const Box*>(dprims), nn, b, nodes, epoch, c->stream), "fit launch");
   }
-  bvh->n = nn;
-  bvh->flags = flags;
-  bvh->kind = kind;
-  bvh->wnodes_valid = false;
-  bvh->codes_valid = true;
-  bvh->prims = dprims;
-  bvh->device = c->device;
-  if (!on_device(prims))
-    return check_device(c); // host caller: finish and report before returning
-  return LBVH_OK;
+  return st;
 }
 
 int
@@ -699,6 +728,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
       if (value < 1 || value > (1 << 24))
         return fail(c, LBVH_ERR_INVALID_ARG, "look-back spin limit %d outside [1, 2^24]", value);
       c->bufs.spin_limit = uint32_t(value);
+      return LBVH_OK;
+    case LBVH_PARAM_SMALL_BUILD_MAX:
+      if (value < 0 || value > int(kSmallMaxPrims))
+        return fail(c, LBVH_ERR_INVALID_ARG, "one-launch build limit %d outside [0, %u]", value, kSmallMaxPrims);
+      c->small_max = uint32_t(value);
       return LBVH_OK;
     case LBVH_PARAM_TEST_TREE_MERGE_CAP:
       if (value < 0 || value > int(kMergeCap))

@@ -10,6 +10,8 @@
 
 #include <atomic>
 
+#include <cooperative_groups.h>
+
 namespace lbvh_gb300 {
 
 // ---------------------------------------------------------------------------
@@ -140,6 +142,18 @@ k_bounds(Leaf leaf, uint32_t n, ArgBox* __restrict__ partials, BuildState* __res
 // sort of large keys-only builds) CTA b takes the codes [b * range, +range)
 // and also writes their counts per bucket of the top 12 bits to row b of
 // `rows`.
+__device__ __forceinline__ uint32_t
+morton_of(const Box& bx, float lo0, float lo1, float lo2, float s0, float s1, float s2)
+{
+  const float cx = fmul(fadd(bx.lo[0], bx.hi[0]), 0.5f);
+  const float cy = fmul(fadd(bx.lo[1], bx.hi[1]), 0.5f);
+  const float cz = fmul(fadd(bx.lo[2], bx.hi[2]), 0.5f);
+  const uint32_t x = __float2uint_rz(fmul(fsub(cx, lo0), s0));
+  const uint32_t y = __float2uint_rz(fmul(fsub(cy, lo1), s1));
+  const uint32_t z = __float2uint_rz(fmul(fsub(cz, lo2), s2));
+  return (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
+}
+
 template<class Leaf, bool kTop>
 __global__ __launch_bounds__(kMortonThreads) void
 k_morton(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes, BuildState* __restrict__ st, uint32_t range,
@@ -159,14 +173,7 @@ k_morton(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes, BuildState* __rest
   const uint32_t stride = kTop ? blockDim.x : gridDim.x * blockDim.x;
   const uint32_t end = kTop ? (n - blockIdx.x * range < range ? n : blockIdx.x * range + range) : n;
   for (uint32_t i = (kTop ? blockIdx.x * range : blockIdx.x * blockDim.x) + threadIdx.x; i < end; i += stride) {
-    const Box bx = leaf(i);
-    const float cx = fmul(fadd(bx.lo[0], bx.hi[0]), 0.5f);
-    const float cy = fmul(fadd(bx.lo[1], bx.hi[1]), 0.5f);
-    const float cz = fmul(fadd(bx.lo[2], bx.hi[2]), 0.5f);
-    const uint32_t x = __float2uint_rz(fmul(fsub(cx, lo0), s0));
-    const uint32_t y = __float2uint_rz(fmul(fsub(cy, lo1), s1));
-    const uint32_t z = __float2uint_rz(fmul(fsub(cz, lo2), s2));
-    const uint32_t code = (expand10(x) << 2) | (expand10(y) << 1) | expand10(z);
+    const uint32_t code = morton_of(leaf(i), lo0, lo1, lo2, s0, s1, s2);
     codes[i] = code;
     atomicAdd(&s_hist[0 * 256 + (code & 255u)], 1u);
     atomicAdd(&s_hist[1 * 256 + ((code >> 8) & 255u)], 1u);
@@ -979,62 +986,30 @@ walk_global(const Leaf& leaf, uint32_t n, const uint32_t* __restrict__ codes, un
   }
 }
 
-template<class Leaf>
-__global__ __launch_bounds__(kTreeThreads) void
-k_tree_local(Leaf leaf,
-             uint32_t n,
-             const uint32_t* __restrict__ codes,
-             Node* __restrict__ nodes,
-             PieceRec* __restrict__ pieces_out,
-             PieceHdr* __restrict__ hdr_out,
-             BuildState* __restrict__ st,
-             unsigned long long* __restrict__ slots,
-             uint32_t epoch,
-             bool walk_on)
+// The local phase's walks over one CTA's kSlots leaf slots [b0, b0 + count):
+// s_delta holds the boundaries b0 - 1 .. b0 + kSlots - 1, s_slot / s_rec
+// start empty, *s_next / *s_npend at 0. Records of the nodes completed here
+// go to s_rec (by Karras index - b0), the CTA roots to s_pend.
+template<uint32_t kSlots, class Leaf>
+__device__ __forceinline__ void
+local_walks(const Leaf& leaf, uint32_t n, uint32_t b0, uint32_t count, const int* s_delta, uint32_t* s_slot,
+            Node* s_rec, PendingNode* s_pend, uint32_t* s_next, uint32_t* s_npend)
 {
-  pdl_begin(); // the predecessor in the stream has finished
-  extern __shared__ __align__(32) unsigned char smem[];
-  int* s_delta = reinterpret_cast<int*>(smem);                               // kTreeBlock + 1
-  uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_delta + kTreeBlock + 8);   // kTreeBlock
-  Node* s_rec = reinterpret_cast<Node*>(s_slot + kTreeBlock);                 // kTreeBlock
-  __shared__ PendingNode s_pend[kTreePendingPerBlock];
-  __shared__ uint32_t s_next, s_npend;
-
-  const uint32_t tid = threadIdx.x, lane = tid & 31;
-  const uint32_t b0 = blockIdx.x * kTreeBlock;
-  const uint32_t count = min(kTreeBlock, n - b0);
-  // A sort that gave up leaves codes in no order, over which a walk could
-  // leave its CTA's ranges: then no tree is built (the error is reported).
-  // The sort kernels have finished, so every thread reads the same bit.
-  const uint32_t sort_failed = __ldcg(&st->error) & kErrLookbackTimeout;
-
-  // boundaries k = b0 - 1 .. b0 + kTreeBlock - 1 at s_delta[k - (b0 - 1)]
-  for (uint32_t j = tid; j <= kTreeBlock; j += kTreeThreads)
-    s_delta[j] = boundary_delta(codes, n, b0 - 1 + j);
-  for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
-    s_slot[j] = kSlotEmpty;
-    s_rec[j].left = 0; // no record (node 0, the root, is never a child)
-  }
-  if (tid == 0) {
-    s_next = 0;
-    s_npend = 0;
-  }
-  __syncthreads();
-  if (sort_failed)
-    return;
-
+  const uint32_t lane = threadIdx.x & 31;
   bool active = false, internal = false;
   uint32_t L = 0, R = 0, lref = 0, rref = 0;
   Box box{};
   const uint32_t lt_mask = (1u << lane) - 1u;
+  bool drained = false; // warp-uniform: the queue had no slot left at this warp's last refill
   for (;;) {
     // ---- lanes without a walk take the next leaf slots of the CTA ----
     const uint32_t idle = __ballot_sync(0xffffffffu, !active);
-    if (idle) {
+    if (idle && !drained) {
       uint32_t first = 0;
       if ((idle & lt_mask) == 0 && !active)
-        first = atomicAdd(&s_next, uint32_t(__popc(idle)));
+        first = atomicAdd(s_next, uint32_t(__popc(idle)));
       first = __shfl_sync(0xffffffffu, first, __ffs(idle) - 1);
+      drained = first + __popc(idle) >= count;
       if (!active) {
         const uint32_t j = first + __popc(idle & lt_mask);
         if (j < count) {
@@ -1055,8 +1030,8 @@ k_tree_local(Leaf leaf,
     const uint32_t s = is_left ? R : L - 1;
     if (internal)
       stage_record(s_rec[(is_left ? R : L) - b0], box, lref, rref);
-    if (s < b0 || s + 1 >= b0 + kTreeBlock) { // split on the CTA's edge
-      const uint32_t k = atomicAdd(&s_npend, 1u);
+    if (s < b0 || s + 1 >= b0 + kSlots) { // split on the CTA's edge
+      const uint32_t k = atomicAdd(s_npend, 1u);
       if (k < kTreePendingPerBlock)
         s_pend[k] = PendingNode{ L, R, box };
       active = false;
@@ -1092,11 +1067,17 @@ k_tree_local(Leaf leaf,
       active = false;
     }
   }
-  __syncthreads();
+}
 
-  // coalesced write-out of the records finished in this CTA, and the first
-  // arrivals that were never matched
-  for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
+// After the walks and a barrier: the coalesced write-out of the records
+// finished in the CTA, and the first arrivals that were never matched (nodes
+// whose sibling range leaves the CTA) added to s_pend.
+template<uint32_t kSlots, class Leaf>
+__device__ __forceinline__ void
+local_write_out(const Leaf& leaf, uint32_t n, uint32_t b0, Node* __restrict__ nodes, const uint32_t* s_slot,
+                const Node* s_rec, PendingNode* s_pend, uint32_t* s_npend)
+{
+  for (uint32_t j = threadIdx.x; j < kSlots; j += blockDim.x) {
     const Node rec = s_rec[j];
     if (rec.left != 0 && b0 + j + 1 < n)
       store_node(nodes, b0 + j, Box{ { rec.lo[0], rec.lo[1], rec.lo[2] }, { rec.hi[0], rec.hi[1], rec.hi[2] } },
@@ -1113,11 +1094,60 @@ k_tree_local(Leaf leaf,
         const Node& o = s_rec[(v <= sj ? wr : wl) - b0];
         wb = Box{ { o.lo[0], o.lo[1], o.lo[2] }, { o.hi[0], o.hi[1], o.hi[2] } };
       }
-      const uint32_t k = atomicAdd(&s_npend, 1u);
+      const uint32_t k = atomicAdd(s_npend, 1u);
       if (k < kTreePendingPerBlock)
         s_pend[k] = PendingNode{ wl, wr, wb };
     }
   }
+}
+
+template<class Leaf>
+__global__ __launch_bounds__(kTreeThreads) void
+k_tree_local(Leaf leaf,
+             uint32_t n,
+             const uint32_t* __restrict__ codes,
+             Node* __restrict__ nodes,
+             PieceRec* __restrict__ pieces_out,
+             PieceHdr* __restrict__ hdr_out,
+             BuildState* __restrict__ st,
+             unsigned long long* __restrict__ slots,
+             uint32_t epoch,
+             bool walk_on)
+{
+  pdl_begin(); // the predecessor in the stream has finished
+  extern __shared__ __align__(32) unsigned char smem[];
+  int* s_delta = reinterpret_cast<int*>(smem);                               // kTreeBlock + 1
+  uint32_t* s_slot = reinterpret_cast<uint32_t*>(s_delta + kTreeBlock + 8);   // kTreeBlock
+  Node* s_rec = reinterpret_cast<Node*>(s_slot + kTreeBlock);                 // kTreeBlock
+  __shared__ PendingNode s_pend[kTreePendingPerBlock];
+  __shared__ uint32_t s_next, s_npend;
+
+  const uint32_t tid = threadIdx.x;
+  const uint32_t b0 = blockIdx.x * kTreeBlock;
+  const uint32_t count = min(kTreeBlock, n - b0);
+  // A sort that gave up leaves codes in no order, over which a walk could
+  // leave its CTA's ranges: then no tree is built (the error is reported).
+  // The sort kernels have finished, so every thread reads the same bit.
+  const uint32_t sort_failed = __ldcg(&st->error) & kErrLookbackTimeout;
+
+  // boundaries k = b0 - 1 .. b0 + kTreeBlock - 1 at s_delta[k - (b0 - 1)]
+  for (uint32_t j = tid; j <= kTreeBlock; j += kTreeThreads)
+    s_delta[j] = boundary_delta(codes, n, b0 - 1 + j);
+  for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
+    s_slot[j] = kSlotEmpty;
+    s_rec[j].left = 0; // no record (node 0, the root, is never a child)
+  }
+  if (tid == 0) {
+    s_next = 0;
+    s_npend = 0;
+  }
+  __syncthreads();
+  if (sort_failed)
+    return;
+
+  local_walks<kTreeBlock>(leaf, n, b0, count, s_delta, s_slot, s_rec, s_pend, &s_next, &s_npend);
+  __syncthreads();
+  local_write_out<kTreeBlock>(leaf, n, b0, nodes, s_slot, s_rec, s_pend, &s_npend);
   __syncthreads();
   const uint32_t np = s_npend;
   if (walk_on) {
@@ -1200,6 +1230,86 @@ group_of(const uint32_t* pre, uint32_t ng, uint32_t i)
       hi = mid;
   }
   return lo;
+}
+
+// The merge's walks over P pieces numbered in leaf order (first leaf L0,
+// delta(L0 - 1) = dL0): s_R / s_d hold each piece's last leaf and the delta
+// after it, s_slot starts empty, piece_box(i) gives piece i's box. Nodes whose
+// parent's split is on the edge (boundary -1 or P - 1) go to s_out.
+template<class PieceBox>
+__device__ __forceinline__ void
+merge_walks(const PieceBox& piece_box, uint32_t n, uint32_t P, uint32_t L0, int dL0, const uint32_t* s_R,
+            const int8_t* s_d, uint32_t* s_slot, Box* s_box, MergeOut* s_out, uint32_t* s_nout,
+            BuildState* __restrict__ st)
+{
+  for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+    Box box = piece_box(i);
+    uint32_t a = i, b = i;
+    uint32_t L = i == 0 ? L0 : s_R[i - 1] + 1, R = s_R[i];
+    int dl = i == 0 ? dL0 : s_d[i - 1], dr = s_d[i];
+    for (uint32_t depth = 0;; depth++) {
+      if (depth > kMaxTreeDepth + 2) {
+        atomicOr(&st->error, kErrBadTopology);
+        break;
+      }
+      const bool is_left = dr > dl; // delta(R) > delta(L - 1)
+      if (is_left ? b + 1 >= P : a == 0) { // the parent's split is on the window's edge
+        const uint32_t j = atomicAdd(s_nout, 1u);
+        if (j < kMergeOut)
+          s_out[j] = MergeOut{ L, R, dr, box };
+        break;
+      }
+      const uint32_t k = is_left ? b : a - 1;
+      s_box[2 * k + (is_left ? 0 : 1)] = box;
+      // release publishes this box, acquire makes the sibling's visible
+      const uint32_t old = arrive_acq_rel_cta(s_slot + k, is_left ? a : b);
+      if (old == kSlotEmpty)
+        break; // first arrival: the sibling completes the parent
+      const Box other = s_box[2 * k + (is_left ? 1 : 0)];
+      box = is_left ? join(box, other) : join(other, box);
+      if (is_left)
+        b = old;
+      else
+        a = old;
+      s_slot[k] = kMergeDone | (a << 16) | b; // read only after the barrier below
+      L = a == 0 ? L0 : s_R[a - 1] + 1;
+      R = s_R[b];
+      if (L == 0 && R == n - 1)
+        break; // the root
+      dl = a == 0 ? dL0 : s_d[a - 1];
+      dr = s_d[b];
+    }
+  }
+}
+
+// After the walks and a barrier: the records of the nodes completed by the
+// walks, and the single arrivals (nodes whose sibling leaves the window) added
+// to s_out.
+__device__ __forceinline__ void
+merge_write_out(uint32_t n, uint32_t P, uint32_t L0, int dL0, const uint32_t* s_R, const int8_t* s_d,
+                const uint32_t* s_slot, const Box* s_box, Node* __restrict__ nodes, MergeOut* s_out, uint32_t* s_nout)
+{
+  for (uint32_t k = threadIdx.x; k + 1 < P; k += blockDim.x) {
+    const uint32_t v = s_slot[k];
+    if (v == kSlotEmpty)
+      continue;
+    if (v & kMergeDone) { // the record of the node completed here
+      const uint32_t a = (v >> 16) & 0x7fffu, b = v & 0xffffu, s = s_R[k];
+      const uint32_t L = a == 0 ? L0 : s_R[a - 1] + 1, R = s_R[b];
+      const uint32_t cl = (L == s) ? (s | kLeafBit) : s;
+      const uint32_t cr = (R == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
+      const int dl = a == 0 ? dL0 : s_d[a - 1];
+      const uint32_t idx = (L == 0 && R == n - 1) ? 0 : (s_d[b] > dl ? R : L);
+      store_node(nodes, idx, join(s_box[2 * k], s_box[2 * k + 1]), cl, cr);
+      continue;
+    }
+    // a single arrival: a node whose sibling range leaves the window
+    const bool left = v <= k; // the waiter covers pieces [v, k] (a left child) or [k + 1, v]
+    const uint32_t a = left ? v : k + 1, b = left ? k : v;
+    const uint32_t j = atomicAdd(s_nout, 1u);
+    if (j < kMergeOut)
+      s_out[j] = MergeOut{ a == 0 ? L0 : s_R[a - 1] + 1, s_R[b], s_d[b], s_box[2 * k + (left ? 0 : 1)] };
+  }
 }
 
 template<class Leaf>
@@ -1292,68 +1402,14 @@ k_tree_merge(Leaf leaf,
   }
   __syncthreads();
 
-  for (uint32_t i = tid; i < P; i += kMergeThreads) {
-    const uint32_t g = group_of(s_pre, ng, i);
-    Box box = load_piece_box(in + size_t(g0 + g) * kMergeOut + (i - s_pre[g]));
-    uint32_t a = i, b = i;
-    uint32_t L = i == 0 ? L0 : s_R[i - 1] + 1, R = s_R[i];
-    int dl = i == 0 ? dL0 : s_d[i - 1], dr = s_d[i];
-    for (uint32_t depth = 0;; depth++) {
-      if (depth > kMaxTreeDepth + 2) {
-        atomicOr(&st->error, kErrBadTopology);
-        break;
-      }
-      const bool is_left = dr > dl; // delta(R) > delta(L - 1)
-      if (is_left ? b + 1 >= P : a == 0) { // the parent's split is on the window's edge
-        const uint32_t j = atomicAdd(&s_nout, 1u);
-        if (j < kMergeOut)
-          s_out[j] = MergeOut{ L, R, dr, box };
-        break;
-      }
-      const uint32_t k = is_left ? b : a - 1;
-      s_box[2 * k + (is_left ? 0 : 1)] = box;
-      // release publishes this box, acquire makes the sibling's visible
-      const uint32_t old = arrive_acq_rel_cta(s_slot + k, is_left ? a : b);
-      if (old == kSlotEmpty)
-        break; // first arrival: the sibling completes the parent
-      const Box other = s_box[2 * k + (is_left ? 1 : 0)];
-      box = is_left ? join(box, other) : join(other, box);
-      if (is_left)
-        b = old;
-      else
-        a = old;
-      s_slot[k] = kMergeDone | (a << 16) | b; // read only after the barrier below
-      L = a == 0 ? L0 : s_R[a - 1] + 1;
-      R = s_R[b];
-      if (L == 0 && R == n - 1)
-        break; // the root
-      dl = a == 0 ? dL0 : s_d[a - 1];
-      dr = s_d[b];
-    }
-  }
+  merge_walks(
+    [&](uint32_t i) {
+      const uint32_t g = group_of(s_pre, ng, i);
+      return load_piece_box(in + size_t(g0 + g) * kMergeOut + (i - s_pre[g]));
+    },
+    n, P, L0, dL0, s_R, s_d, s_slot, s_box, s_out, &s_nout, st);
   __syncthreads();
-
-  for (uint32_t k = tid; k + 1 < P; k += kMergeThreads) {
-    const uint32_t v = s_slot[k];
-    if (v == kSlotEmpty)
-      continue;
-    if (v & kMergeDone) { // the record of the node completed here
-      const uint32_t a = (v >> 16) & 0x7fffu, b = v & 0xffffu, s = s_R[k];
-      const uint32_t L = a == 0 ? L0 : s_R[a - 1] + 1, R = s_R[b];
-      const uint32_t cl = (L == s) ? (s | kLeafBit) : s;
-      const uint32_t cr = (R == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
-      const int dl = a == 0 ? dL0 : s_d[a - 1];
-      const uint32_t idx = (L == 0 && R == n - 1) ? 0 : (s_d[b] > dl ? R : L);
-      store_node(nodes, idx, join(s_box[2 * k], s_box[2 * k + 1]), cl, cr);
-      continue;
-    }
-    // a single arrival: a node whose sibling range leaves the window
-    const bool left = v <= k; // the waiter covers pieces [v, k] (a left child) or [k + 1, v]
-    const uint32_t a = left ? v : k + 1, b = left ? k : v;
-    const uint32_t j = atomicAdd(&s_nout, 1u);
-    if (j < kMergeOut)
-      s_out[j] = MergeOut{ a == 0 ? L0 : s_R[a - 1] + 1, s_R[b], s_d[b], s_box[2 * k + (left ? 0 : 1)] };
-  }
+  merge_write_out(n, P, L0, dL0, s_R, s_d, s_slot, s_box, nodes, s_out, &s_nout);
   __syncthreads();
   const uint32_t nout = s_nout;
   if (last) {
@@ -1374,6 +1430,301 @@ k_tree_merge(Leaf leaf,
       rank += s_out[j].L < o.L;
     store_piece(out + size_t(blockIdx.x) * kMergeOut + rank, o.R, o.dR, o.box);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Small keys-only builds in one launch (k_small_build). One thread-block
+// cluster of C = ceil(n / 1024) CTAs (C <= 16); CTA r holds primitives and
+// leaf slots [1024 r, 1024 r + 1024) -- in parity mode leaf slot p is
+// primitive p, so a CTA's leaf boxes are the boxes it computes. Every phase
+// is the multi-kernel build's arithmetic, in shared memory:
+//   1. the leaf boxes and the centroid bounds with the index tie rule
+//      (k_bounds); the CTAs' partial bounds are combined through distributed
+//      shared memory;
+//   2. the Morton codes (k_morton);
+//   3. four stable 8-bit LSD passes over the cluster: each CTA ranks its keys
+//      per warp (__match_any_sync), publishes its digit counts, reads every
+//      CTA's counts to find its keys' global positions, and stores each key
+//      into the shared memory of the CTA that owns that position;
+//   4. the local tree phase over the CTA's 1,024 slots (local_walks), with the
+//      neighbours' edge codes read remotely, its pieces kept in shared memory;
+//   5. CTA 0 gathers every CTA's pieces and merges them to the root
+//      (merge_walks), as the last merge level does.
+// A cluster barrier separates the phases that read other CTAs' shared memory.
+namespace cg = cooperative_groups;
+
+struct SmemLeaf
+{
+  const Box* boxes;
+  uint32_t b0;
+  __device__ __forceinline__ Box operator()(uint32_t i) const { return boxes[i - b0]; }
+};
+
+template<class Leaf>
+__global__ __launch_bounds__(kSmallThreads, 1) void
+k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __restrict__ nodes,
+              BuildState* __restrict__ st)
+{
+  pdl_begin(); // the predecessor in the stream has finished
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(32) unsigned char smem[];
+  Box* s_box = reinterpret_cast<Box*>(smem + kSmBox);
+  uint32_t* s_key = reinterpret_cast<uint32_t*>(smem + kSmKey);
+  __shared__ uint32_t s_hist[256], s_tot[256], s_before[256], s_base[256];
+  PieceRec* s_piece = reinterpret_cast<PieceRec*>(smem + kSmPiece);
+  unsigned char* u = smem + kSmUnion;
+  __shared__ ArgBox s_part[kSmallThreads / 32];
+  __shared__ ArgBox s_cpart;
+  __shared__ float s_lo[3], s_scale[3];
+  __shared__ uint32_t s_next, s_npend, s_npieces, s_nout;
+  __shared__ uint32_t s_pre[kSmallMaxCtas + 1];
+
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t r = blockIdx.x, C = gridDim.x; // the grid is one cluster
+  const uint32_t b0 = r * kSmallSlots, cnt = min(kSmallSlots, n - b0);
+  const bool valid = tid < cnt;
+
+  // ---- 1. leaf boxes and centroid bounds (k_bounds) ----
+  ArgBox a = empty_arg();
+  Box bx{};
+  if (valid) {
+    const uint32_t i = b0 + tid;
+    bx = leaf(i);
+    s_box[tid] = bx;
+    const float c[3] = { fmul(fadd(bx.lo[0], bx.hi[0]), 0.5f), fmul(fadd(bx.lo[1], bx.hi[1]), 0.5f),
+                         fmul(fadd(bx.lo[2], bx.hi[2]), 0.5f) };
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      if (c[k] < a.v[k]) {
+        a.v[k] = c[k];
+        a.i[k] = i;
+      }
+      if (a.v[k + 3] < c[k]) {
+        a.v[k + 3] = c[k];
+        a.i[k + 3] = i;
+      }
+    }
+  }
+  a = block_reduce_arg(a, s_part);
+  if (tid == 0)
+    s_cpart = a;
+  cluster.sync();
+  if (warp == 0) { // lane q takes CTA q's partial; the combine is order-free
+    ArgBox t = lane < C ? *cluster.map_shared_rank(&s_cpart, lane) : empty_arg();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ArgBox o2;
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        o2.v[k] = __shfl_down_sync(0xffffffffu, t.v[k], o);
+        o2.i[k] = __shfl_down_sync(0xffffffffu, t.i[k], o);
+      }
+      combine(t, o2);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        s_lo[k] = t.v[k];
+        s_scale[k] = fdiv(1024.0f, fadd(fsub(t.v[k + 3], t.v[k]), 1.0f)); // lbvh.h:1437-1441
+      }
+  }
+  __syncthreads();
+
+  // ---- 2. Morton codes (k_morton) ----
+  uint32_t* key_cur = s_key;
+  uint32_t* key_nxt = s_key + kSmallSlots;
+  if (valid)
+    key_cur[tid] = morton_of(bx, s_lo[0], s_lo[1], s_lo[2], s_scale[0], s_scale[1], s_scale[2]);
+
+  // ---- 3. four stable 8-bit LSD passes over the cluster ----
+  uint16_t* s_wcnt = reinterpret_cast<uint16_t*>(u);                  // [32 warps][256 digits]
+  uint32_t* s_quarter = reinterpret_cast<uint32_t*>(u + 32 * 256 * 2); // [4 quarters of 8 warps][256]
+  for (int pass = 0; pass < 4; pass++) {
+    for (uint32_t k = tid; k < 32 * 256 / 2; k += kSmallThreads)
+      reinterpret_cast<uint32_t*>(s_wcnt)[k] = 0;
+    __syncthreads();
+    const uint32_t key = valid ? key_cur[tid] : 0u;
+    const uint32_t d = (key >> (8 * pass)) & 255u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
+    const uint32_t rank_w = __popc(peers & ((1u << lane) - 1u));
+    if (valid && rank_w == 0)
+      s_wcnt[warp * 256 + d] = uint16_t(__popc(peers));
+    __syncthreads();
+    { // per digit and quarter of the warps: the warps' exclusive prefix
+      const uint32_t dg = tid & 255u, qt = tid >> 8;
+      uint32_t run = 0;
+#pragma unroll
+      for (int w = 0; w < 8; w++) {
+        const uint32_t c = s_wcnt[(qt * 8 + w) * 256 + dg];
+        s_wcnt[(qt * 8 + w) * 256 + dg] = uint16_t(run);
+        run += c;
+      }
+      s_quarter[qt * 256 + dg] = run;
+    }
+    __syncthreads();
+    { // add the earlier quarters; the CTA's count of each digit to s_hist
+      const uint32_t dg = tid & 255u, qt = tid >> 8;
+      uint32_t off = 0;
+      for (uint32_t k = 0; k < qt; k++)
+        off += s_quarter[k * 256 + dg];
+      if (off)
+#pragma unroll
+        for (int w = 0; w < 8; w++)
+          s_wcnt[(qt * 8 + w) * 256 + dg] += uint16_t(off);
+      if (qt == 0)
+        s_hist[dg] = s_quarter[dg] + s_quarter[256 + dg] + s_quarter[512 + dg] + s_quarter[768 + dg];
+    }
+    cluster.sync(); // every CTA's digit counts are complete
+    if (tid < 256) { // every CTA's count of this digit, read in parallel
+      uint32_t h[kSmallMaxCtas];
+#pragma unroll
+      for (uint32_t q = 0; q < kSmallMaxCtas; q++)
+        h[q] = q < C ? cluster.map_shared_rank(s_hist, q)[tid] : 0u;
+      uint32_t tot = 0, before = 0;
+#pragma unroll
+      for (uint32_t q = 0; q < kSmallMaxCtas; q++) {
+        tot += h[q];
+        before += q < r ? h[q] : 0u;
+      }
+      s_tot[tid] = tot;
+      s_before[tid] = before;
+    }
+    __syncthreads();
+    if (warp == 0) { // exclusive scan of the 256 digit totals: 8 per lane
+      uint32_t t8[8], sum = 0;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        t8[k] = s_tot[lane * 8 + k];
+        sum += t8[k];
+      }
+      uint32_t x = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= uint32_t(o))
+          x += y;
+      }
+      uint32_t ex = x - sum;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        s_base[lane * 8 + k] = ex + s_before[lane * 8 + k];
+        ex += t8[k];
+      }
+    }
+    __syncthreads();
+    if (valid) {
+      const uint32_t pos = s_base[d] + s_wcnt[warp * 256 + d] + rank_w; // < n by construction
+      if (pos < n)
+        cluster.map_shared_rank(key_nxt, pos / kSmallSlots)[pos % kSmallSlots] = key;
+      else
+        atomicOr(&st->error, kErrBadTopology);
+    }
+    cluster.sync(); // every key has landed and every count has been read
+    uint32_t* t = key_cur;
+    key_cur = key_nxt;
+    key_nxt = t;
+  }
+
+  // ---- 4. local tree phase over the CTA's slots ----
+  int* s_delta = reinterpret_cast<int*>(u);
+  uint32_t* s_slot = reinterpret_cast<uint32_t*>(u + kSmTreeSlot);
+  Node* s_rec = reinterpret_cast<Node*>(u + kSmTreeRec);
+  PendingNode* s_pend = reinterpret_cast<PendingNode*>(u + kSmTreePend);
+  {
+    // boundary b0 - 1 + tid, and (thread 0) b0 + 1023; codes beyond the CTA
+    // are the neighbours' edge codes
+    const auto code_at = [&](uint32_t k) -> uint32_t {
+      if (k < b0)
+        return *cluster.map_shared_rank(key_cur + (kSmallSlots - 1), r - 1);
+      if (k >= b0 + kSmallSlots)
+        return *cluster.map_shared_rank(key_cur, r + 1);
+      return key_cur[k - b0];
+    };
+    for (uint32_t j = tid; j <= kSmallSlots; j += kSmallThreads) {
+      const uint32_t k = b0 - 1 + j;
+      int dv = -1; // k = L - 1 wraps for L = 0; k >= n - 1 is past the end
+      if (k < n - 1) {
+        const uint32_t x = code_at(k), y = code_at(k + 1);
+        dv = x == y ? int(__clz(k ^ (k + 1))) + 32 : int(__clz(x ^ y));
+      }
+      s_delta[j] = dv;
+    }
+    s_slot[tid] = kSlotEmpty;
+    s_rec[tid].left = 0; // no record (node 0, the root, is never a child)
+    if (tid == 0) {
+      s_next = 0;
+      s_npend = 0;
+    }
+  }
+  __syncthreads();
+  const SmemLeaf sl{ s_box, b0 };
+  local_walks<kSmallSlots>(sl, n, b0, cnt, s_delta, s_slot, s_rec, s_pend, &s_next, &s_npend);
+  __syncthreads();
+  local_write_out<kSmallSlots>(sl, n, b0, nodes, s_slot, s_rec, s_pend, &s_npend);
+  __syncthreads();
+  {
+    const uint32_t np = s_npend, m = min(np, kMergeOut);
+    if (tid == 0) {
+      if (np > kMergeOut)
+        atomicOr(&st->error, kErrBadTopology); // more canonical pieces than a tree can have
+      s_npieces = m;
+    }
+    for (uint32_t k = tid; k < m; k += kSmallThreads) {
+      const PendingNode pn = s_pend[k];
+      uint32_t rank = 0; // the pieces partition the CTA's slots: their first leaves differ
+      for (uint32_t j = 0; j < m; j++)
+        rank += s_pend[j].L < pn.L;
+      store_piece(s_piece + rank, pn.R, s_delta[pn.R - b0 + 1], pn.box);
+    }
+  }
+  cluster.sync(); // every CTA's pieces are complete
+
+  // ---- 5. CTA 0 gathers the pieces and merges them to the root ----
+  Box* m_box = reinterpret_cast<Box*>(u);
+  uint32_t* m_R = reinterpret_cast<uint32_t*>(u + kSmMergeR);
+  uint32_t* m_slot = reinterpret_cast<uint32_t*>(u + kSmMergeSlot);
+  int8_t* m_d = reinterpret_cast<int8_t*>(u + kSmMergeD);
+  MergeOut* m_out = reinterpret_cast<MergeOut*>(u + kSmMergeOut);
+  const bool merging = r == 0 && C > 1;
+  if (merging) { // this CTA's tree scratch is dead: its write-out ended before the barrier
+    if (warp == 0) { // lane q reads CTA q's piece count; a running sum gives the starts
+      uint32_t v = lane < C ? *cluster.map_shared_rank(&s_npieces, lane) : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= uint32_t(o))
+          v += y;
+      }
+      if (lane < C)
+        s_pre[lane + 1] = v;
+      if (lane == 0) {
+        s_pre[0] = 0;
+        s_nout = 0;
+      }
+    }
+    __syncthreads();
+    const uint32_t P = s_pre[C];
+    for (uint32_t i = tid; i < P; i += kSmallThreads) {
+      const uint32_t q = group_of(s_pre, C, i);
+      const PieceRec* pr = cluster.map_shared_rank(s_piece, q) + (i - s_pre[q]);
+      m_R[i] = pr->R;
+      m_d[i] = int8_t(pr->dR);
+      m_slot[i] = kSlotEmpty;
+      m_box[2 * i] = pr->box; // piece i's box: only a node containing piece i writes there later
+    }
+  }
+  cluster.sync(); // CTA 0 has read every CTA's pieces: the others may exit
+  if (valid) // the sorted codes, for refits (stored last: no store is in flight during the walks)
+    codes_out[b0 + tid] = key_cur[tid];
+  if (!merging)
+    return;
+  const uint32_t P = s_pre[C];
+  merge_walks([&](uint32_t i) { return m_box[2 * i]; }, n, P, 0u, -1, m_R, m_d, m_slot, m_box, m_out, &s_nout, st);
+  __syncthreads();
+  merge_write_out(n, P, 0u, -1, m_R, m_d, m_slot, m_box, nodes, m_out, &s_nout);
+  __syncthreads();
+  if (tid == 0 && s_nout != 0)
+    atomicOr(&st->error, kErrBadTopology); // the root was not reached
 }
 
 // Parent links from an existing node array (for refit).
@@ -1663,6 +2014,89 @@ launch_topology_and_fit(const Leaf& leaf, uint32_t n, const BuildBuffers& b, Nod
                         ts.window[lv], pieces(lv + 1), hdrs(lv + 1), pieces(0), hdrs(0), ts.groups[0], cap, last));
   }
   return cudaGetLastError();
+}
+
+template<class Leaf>
+static cudaError_t
+launch_small(const Leaf& leaf, uint32_t n, uint32_t* codes_out, Node* nodes, BuildState* st, cudaStream_t s)
+{
+  const uint32_t C = ceil_div_u32(n, kSmallSlots);
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(kSmallThreads);
+  cfg.dynamicSmemBytes = kSmallSmem;
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 2;
+  return cudaLaunchKernelEx(&cfg, k_small_build<Leaf>, leaf, n, codes_out, nodes, st);
+}
+
+// Per device: the shared-memory and cluster-size opt-ins of both
+// instantiations, then the largest cluster (16, else 8 CTAs) the device can
+// schedule with this much shared memory per CTA.
+uint32_t
+small_build_limit()
+{
+  static std::atomic<uint32_t> limit[64];
+  static std::atomic<uint64_t> known{ 0 };
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 0;
+  }
+  const uint64_t bit = 1ull << dev;
+  if (known.load(std::memory_order_acquire) & bit)
+    return limit[dev].load(std::memory_order_relaxed);
+  uint32_t best = 0;
+  auto setup = [](auto kernel) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmallSmem)) == cudaSuccess &&
+           cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+  };
+  if (setup(k_small_build<TriLeaf>) && setup(k_small_build<BoxLeaf>)) {
+    for (uint32_t c : { kSmallMaxCtas, 8u }) {
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = c;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(c);
+      cfg.blockDim = dim3(kSmallThreads);
+      cfg.dynamicSmemBytes = kSmallSmem;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      int tri = 0, box = 0;
+      if (cudaOccupancyMaxActiveClusters(&tri, k_small_build<TriLeaf>, &cfg) == cudaSuccess &&
+          cudaOccupancyMaxActiveClusters(&box, k_small_build<BoxLeaf>, &cfg) == cudaSuccess && tri > 0 && box > 0) {
+        best = c * kSmallSlots;
+        break;
+      }
+    }
+  }
+  cudaGetLastError(); // a refused opt-in or query only disables this path
+  limit[dev].store(best, std::memory_order_relaxed);
+  known.fetch_or(bit, std::memory_order_release);
+  return best;
+}
+
+cudaError_t
+launch_small_build_tris(const Tri* tris, uint32_t n, uint32_t* codes_out, Node* nodes, BuildState* st, cudaStream_t s)
+{
+  return launch_small(TriLeaf{ tris }, n, codes_out, nodes, st, s);
+}
+
+cudaError_t
+launch_small_build_boxes(const Box* boxes, uint32_t n, uint32_t* codes_out, Node* nodes, BuildState* st,
+                         cudaStream_t s)
+{
+  return launch_small(BoxLeaf{ boxes }, n, codes_out, nodes, st, s);
 }
 
 cudaError_t

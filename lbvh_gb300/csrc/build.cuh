@@ -141,6 +141,39 @@ tree_scratch(size_t n)
   return t;
 }
 
+// Keys-only builds of up to kSmallMaxPrims primitives run as one launch of
+// k_small_build: a thread-block cluster of ceil(n / kSmallSlots) CTAs, each
+// holding kSmallSlots primitives' boxes and codes in shared memory, which
+// computes the bounds, the codes, the sort (over distributed shared memory),
+// the local tree phase and (CTA 0) the merge without touching global memory
+// in between.
+constexpr uint32_t kSmallSlots = 1024;
+constexpr int kSmallThreads = 1024;
+constexpr uint32_t kSmallMaxCtas = 16; // a non-portable cluster size, checked per device
+constexpr uint32_t kSmallMaxPrims = kSmallSlots * kSmallMaxCtas;
+constexpr uint32_t kSmallMergeCap = kSmallMaxCtas * kMergeOut; // every piece of every CTA
+// shared memory of k_small_build, byte offsets (each part on 32 bytes)
+constexpr size_t kSmBox = 0;                                   // Box[kSmallSlots]: leaf boxes
+constexpr size_t kSmKey = kSmBox + kSmallSlots * 24;           // uint32[2][kSmallSlots]: codes
+constexpr size_t kSmPiece = kSmKey + 2 * kSmallSlots * 4;      // PieceRec[kMergeOut]: the CTA's pieces
+constexpr size_t kSmUnion = kSmPiece + kMergeOut * 32;         // sort, tree or merge scratch:
+// tree: int[kSmallSlots + 8] deltas, uint32[kSmallSlots] slots, Node[kSmallSlots], PendingNode[kMergeOut]
+constexpr size_t kSmTreeSlot = (kSmallSlots + 8) * 4 + 32;
+constexpr size_t kSmTreeRec = kSmTreeSlot + kSmallSlots * 4 + 32;
+constexpr size_t kSmTreePend = kSmTreeRec + kSmallSlots * 32;
+constexpr size_t kSmTree = kSmTreePend + kMergeOut * 32;
+// merge: Box[2 x kSmallMergeCap] child boxes (piece i's own box at 2i first), uint32 ends, uint32 slots,
+// int8 deltas, MergeOut[kMergeOut]
+constexpr size_t kSmMergeR = size_t(kSmallMergeCap) * 2 * 24;
+constexpr size_t kSmMergeSlot = kSmMergeR + kSmallMergeCap * 4;
+constexpr size_t kSmMergeD = kSmMergeSlot + kSmallMergeCap * 4;
+constexpr size_t kSmMergeOut = kSmMergeD + kSmallMergeCap;
+constexpr size_t kSmMerge = kSmMergeOut + kMergeOut * 48;
+constexpr size_t kSmSort = 32 * 256 * 2 + 4 * 256 * 4; // uint16[32 warps][256 digits], uint32[4][256]
+constexpr size_t kSmallSmem =
+  kSmUnion + (kSmMerge > kSmTree ? (kSmMerge > kSmSort ? kSmMerge : kSmSort) : (kSmTree > kSmSort ? kSmTree : kSmSort));
+static_assert(kSmUnion % 32 == 0 && kSmPiece % 32 == 0 && kSmTreeRec % 32 == 0, "small build smem alignment");
+
 // Per-leaf box sources for the templated build kernels.
 struct TriLeaf
 {
@@ -195,6 +228,15 @@ struct BuildBuffers
 };
 
 cudaError_t launch_make_triangles(const float* verts, uint32_t n, Tri* out, cudaStream_t s);
+// Largest keys-only build k_small_build runs on the current device (0 when
+// its cluster cannot be scheduled there); checked once per device.
+uint32_t small_build_limit();
+// The whole keys-only build of n <= small_build_limit() primitives in one
+// launch: sorted codes to codes_out, nodes to `nodes`, errors to st->error.
+cudaError_t launch_small_build_tris(const Tri* tris, uint32_t n, uint32_t* codes_out, Node* nodes, BuildState* st,
+                                    cudaStream_t s);
+cudaError_t launch_small_build_boxes(const Box* boxes, uint32_t n, uint32_t* codes_out, Node* nodes, BuildState* st,
+                                     cudaStream_t s);
 // Bounds + Morton codes; with b.boxes set, also stages the leaf boxes there
 // (input order) so the Morton pass and launch_fit_staged read 24 bytes per
 // leaf instead of the 48-byte triangle.

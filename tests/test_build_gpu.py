@@ -58,7 +58,8 @@ def test_build_matches_oracle_random(ctx, port, n):
     ref_nodes = port.build(t, 8)
     assert nodes_equal(bvh.nodes(), ref_nodes)
     assert port.check_bvh(bvh.nodes()) == 0
-    # keys-only sort (one-CTA sort up to 20,480 codes, onesweep passes above)
+    # keys-only build (one cluster launch up to 16,384 primitives, the
+    # multi-kernel build above)
     assert nodes_equal(lb.Builder(ctx)(dev(t)).nodes(), ref_nodes)
     sl = lb.Builder(ctx, sorted_leaves=True)(dev(t))
     assert nodes_equal(sl.nodes(), port.build(t[perm], 8))
@@ -202,6 +203,35 @@ def test_sort_and_bounds_parameters(lib_built, port, tile, bucket_min, bounds):
                        (_lib.PARAM_BOUNDS_BLOCKS_PER_SM, 17)):
         with pytest.raises(ValueError):
             c.set_param(param, bad)
+
+
+@pytest.mark.parametrize("n", [2, 3, 1023, 1024, 1025, 2048, 7777, 8193, 16383, 16384, 16385])
+def test_one_launch_build_matches_multi_kernel(lib_built, port, n):
+    """Keys-only builds of up to 16,384 primitives run as one cluster launch
+    (LBVH_PARAM_SMALL_BUILD_MAX); at 0 they take the multi-kernel build. Both
+    give the reference's nodes, for triangles (host and device input) and for
+    boxes, on random soups and on duplicate-heavy input."""
+    from lbvh_gb300 import _lib
+
+    one = lb.Context()
+    multi = lb.Context()
+    multi.set_param(_lib.PARAM_SMALL_BUILD_MAX, 0)
+    for t in (scenes.soup(n, seed=n + 5), np.repeat(scenes.soup((n + 6) // 7, seed=n)[:, None], 7, 1)
+              .reshape(-1, 12)[:n].copy()):
+        if t.shape[0] < 2:
+            continue
+        want = port.build(t, 8)
+        for c in (one, multi):
+            assert nodes_equal(lb.Builder(c)(dev(t)).nodes(), want), (n, c is one)
+            assert nodes_equal(lb.Builder(c)(t).nodes(), want), (n, c is one)
+        boxes = port.tri_boxes(t)
+        want_b = port.build_boxes(boxes, 8)
+        for c in (one, multi):
+            assert nodes_equal(lb.Builder(c)(dev(boxes), converter=lb.BOXES).nodes(), want_b), (n, c is one)
+    torus = scenes.torus_scene(seed=3)
+    assert nodes_equal(lb.Builder(one)(dev(torus)).nodes(), port.build(torus, 8))
+    with pytest.raises(ValueError):
+        one.set_param(_lib.PARAM_SMALL_BUILD_MAX, 16385)
 
 
 @pytest.mark.parametrize("fused,merge_cap", [(0, 0), (1, 0), (0, 8)])
