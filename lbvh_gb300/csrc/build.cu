@@ -1053,8 +1053,7 @@ local_walks(const Leaf& leaf, uint32_t n, uint32_t b0, uint32_t count, const int
     if (sib & kLeafBit) {
       other = leaf(sib & ~kLeafBit);
     } else {
-      const Node& o = s_rec[sib - b0];
-      other = Box{ { o.lo[0], o.lo[1], o.lo[2] }, { o.hi[0], o.hi[1], o.hi[2] } };
+      other = staged_box(s_rec[sib - b0]);
     }
     box = is_left ? join(box, other) : join(other, box);
     L = LP;
@@ -1260,12 +1259,12 @@ merge_walks(const PieceBox& piece_box, uint32_t n, uint32_t P, uint32_t L0, int 
         break;
       }
       const uint32_t k = is_left ? b : a - 1;
-      s_box[2 * k + (is_left ? 0 : 1)] = box;
+      store_box8(s_box + 2 * k + (is_left ? 0 : 1), box);
       // release publishes this box, acquire makes the sibling's visible
       const uint32_t old = arrive_acq_rel_cta(s_slot + k, is_left ? a : b);
       if (old == kSlotEmpty)
         break; // first arrival: the sibling completes the parent
-      const Box other = s_box[2 * k + (is_left ? 1 : 0)];
+      const Box other = load_box8(s_box + 2 * k + (is_left ? 1 : 0));
       box = is_left ? join(box, other) : join(other, box);
       if (is_left)
         b = old;
@@ -1300,7 +1299,7 @@ merge_write_out(uint32_t n, uint32_t P, uint32_t L0, int dL0, const uint32_t* s_
       const uint32_t cr = (R == s + 1) ? ((s + 1) | kLeafBit) : (s + 1);
       const int dl = a == 0 ? dL0 : s_d[a - 1];
       const uint32_t idx = (L == 0 && R == n - 1) ? 0 : (s_d[b] > dl ? R : L);
-      store_node(nodes, idx, join(s_box[2 * k], s_box[2 * k + 1]), cl, cr);
+      store_node(nodes, idx, join(load_box8(s_box + 2 * k), load_box8(s_box + 2 * k + 1)), cl, cr);
       continue;
     }
     // a single arrival: a node whose sibling range leaves the window
@@ -1457,7 +1456,7 @@ struct SmemLeaf
 {
   const Box* boxes;
   uint32_t b0;
-  __device__ __forceinline__ Box operator()(uint32_t i) const { return boxes[i - b0]; }
+  __device__ __forceinline__ Box operator()(uint32_t i) const { return load_box8(boxes + (i - b0)); }
 };
 
 template<class Leaf>
@@ -1470,7 +1469,7 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   extern __shared__ __align__(32) unsigned char smem[];
   Box* s_box = reinterpret_cast<Box*>(smem + kSmBox);
   uint32_t* s_key = reinterpret_cast<uint32_t*>(smem + kSmKey);
-  __shared__ uint32_t s_hist[256], s_tot[256], s_before[256], s_base[256];
+  __shared__ uint32_t s_hist[1024], s_base[1024], s_wsum[32];
   PieceRec* s_piece = reinterpret_cast<PieceRec*>(smem + kSmPiece);
   unsigned char* u = smem + kSmUnion;
   __shared__ ArgBox s_part[kSmallThreads / 32];
@@ -1490,7 +1489,7 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   if (valid) {
     const uint32_t i = b0 + tid;
     bx = leaf(i);
-    s_box[tid] = bx;
+    store_box8(s_box + tid, bx);
     const float c[3] = { fmul(fadd(bx.lo[0], bx.hi[0]), 0.5f), fmul(fadd(bx.lo[1], bx.hi[1]), 0.5f),
                          fmul(fadd(bx.lo[2], bx.hi[2]), 0.5f) };
 #pragma unroll
@@ -1536,90 +1535,81 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   if (valid)
     key_cur[tid] = morton_of(bx, s_lo[0], s_lo[1], s_lo[2], s_scale[0], s_scale[1], s_scale[2]);
 
-  // ---- 3. four stable 8-bit LSD passes over the cluster ----
-  uint16_t* s_wcnt = reinterpret_cast<uint16_t*>(u);                  // [32 warps][256 digits]
-  uint32_t* s_quarter = reinterpret_cast<uint32_t*>(u + 32 * 256 * 2); // [4 quarters of 8 warps][256]
-  for (int pass = 0; pass < 4; pass++) {
-    for (uint32_t k = tid; k < 32 * 256 / 2; k += kSmallThreads)
-      reinterpret_cast<uint32_t*>(s_wcnt)[k] = 0;
+  // ---- 3. three stable 10-bit LSD passes over the cluster (codes are 30 bits) ----
+  uint16_t* s_wcnt = reinterpret_cast<uint16_t*>(u); // [32 warps][1024 digits]
+  for (uint32_t k = tid; k < 32 * 1024 / 2; k += kSmallThreads)
+    reinterpret_cast<uint32_t*>(s_wcnt)[k] = 0;
+  for (int pass = 0; pass < 3; pass++) {
     __syncthreads();
     const uint32_t key = valid ? key_cur[tid] : 0u;
-    const uint32_t d = (key >> (8 * pass)) & 255u;
-    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
+    const uint32_t d = (key >> (10 * pass)) & 1023u;
+    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 1024u + lane);
     const uint32_t rank_w = __popc(peers & ((1u << lane) - 1u));
     if (valid && rank_w == 0)
-      s_wcnt[warp * 256 + d] = uint16_t(__popc(peers));
+      s_wcnt[warp * 1024 + d] = uint16_t(__popc(peers));
     __syncthreads();
-    { // per digit and quarter of the warps: the warps' exclusive prefix
-      const uint32_t dg = tid & 255u, qt = tid >> 8;
+    { // digit tid: the warps' exclusive prefix, and the CTA's count
       uint32_t run = 0;
-#pragma unroll
-      for (int w = 0; w < 8; w++) {
-        const uint32_t c = s_wcnt[(qt * 8 + w) * 256 + dg];
-        s_wcnt[(qt * 8 + w) * 256 + dg] = uint16_t(run);
+#pragma unroll 8
+      for (int w = 0; w < 32; w++) {
+        const uint32_t c = s_wcnt[w * 1024 + tid];
+        s_wcnt[w * 1024 + tid] = uint16_t(run);
         run += c;
       }
-      s_quarter[qt * 256 + dg] = run;
-    }
-    __syncthreads();
-    { // add the earlier quarters; the CTA's count of each digit to s_hist
-      const uint32_t dg = tid & 255u, qt = tid >> 8;
-      uint32_t off = 0;
-      for (uint32_t k = 0; k < qt; k++)
-        off += s_quarter[k * 256 + dg];
-      if (off)
-#pragma unroll
-        for (int w = 0; w < 8; w++)
-          s_wcnt[(qt * 8 + w) * 256 + dg] += uint16_t(off);
-      if (qt == 0)
-        s_hist[dg] = s_quarter[dg] + s_quarter[256 + dg] + s_quarter[512 + dg] + s_quarter[768 + dg];
+      s_hist[tid] = run;
     }
     cluster.sync(); // every CTA's digit counts are complete
-    if (tid < 256) { // every CTA's count of this digit, read in parallel
+    uint32_t tot = 0, before = 0;
+    { // every CTA's count of this digit, read in parallel
       uint32_t h[kSmallMaxCtas];
 #pragma unroll
       for (uint32_t q = 0; q < kSmallMaxCtas; q++)
         h[q] = q < C ? cluster.map_shared_rank(s_hist, q)[tid] : 0u;
-      uint32_t tot = 0, before = 0;
 #pragma unroll
       for (uint32_t q = 0; q < kSmallMaxCtas; q++) {
         tot += h[q];
         before += q < r ? h[q] : 0u;
       }
-      s_tot[tid] = tot;
-      s_before[tid] = before;
     }
-    __syncthreads();
-    if (warp == 0) { // exclusive scan of the 256 digit totals: 8 per lane
-      uint32_t t8[8], sum = 0;
-#pragma unroll
-      for (int k = 0; k < 8; k++) {
-        t8[k] = s_tot[lane * 8 + k];
-        sum += t8[k];
-      }
-      uint32_t x = sum;
+    { // exclusive scan of the 1,024 digit totals
+      uint32_t x = tot;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= uint32_t(o))
           x += y;
       }
-      uint32_t ex = x - sum;
+      if (lane == 31)
+        s_wsum[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        const uint32_t w = s_wsum[lane];
+        uint32_t t = w;
 #pragma unroll
-      for (int k = 0; k < 8; k++) {
-        s_base[lane * 8 + k] = ex + s_before[lane * 8 + k];
-        ex += t8[k];
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+          if (lane >= uint32_t(o))
+            t += y;
+        }
+        s_wsum[lane] = t - w;
       }
+      __syncthreads();
+      s_base[tid] = x - tot + s_wsum[warp] + before;
     }
     __syncthreads();
     if (valid) {
-      const uint32_t pos = s_base[d] + s_wcnt[warp * 256 + d] + rank_w; // < n by construction
+      const uint32_t pos = s_base[d] + s_wcnt[warp * 1024 + d] + rank_w; // < n by construction
       if (pos < n)
         cluster.map_shared_rank(key_nxt, pos / kSmallSlots)[pos % kSmallSlots] = key;
       else
         atomicOr(&st->error, kErrBadTopology);
     }
-    cluster.sync(); // every key has landed and every count has been read
+    // every key has landed and every count has been read once all CTAs
+    // arrive; the next pass's warp counts are cleared meanwhile
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    for (uint32_t k = tid; k < 32 * 1024 / 2; k += kSmallThreads)
+      reinterpret_cast<uint32_t*>(s_wcnt)[k] = 0;
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     uint32_t* t = key_cur;
     key_cur = key_nxt;
     key_nxt = t;
@@ -1707,10 +1697,12 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
     for (uint32_t i = tid; i < P; i += kSmallThreads) {
       const uint32_t q = group_of(s_pre, C, i);
       const PieceRec* pr = cluster.map_shared_rank(s_piece, q) + (i - s_pre[q]);
-      m_R[i] = pr->R;
-      m_d[i] = int8_t(pr->dR);
+      const float4 pa = reinterpret_cast<const float4*>(pr)[0], pb = reinterpret_cast<const float4*>(pr)[1];
+      m_R[i] = __float_as_uint(pa.x);
+      m_d[i] = int8_t(__float_as_int(pa.y));
       m_slot[i] = kSlotEmpty;
-      m_box[2 * i] = pr->box; // piece i's box: only a node containing piece i writes there later
+      // piece i's box: only a node containing piece i writes there later
+      store_box8(m_box + 2 * i, Box{ { pa.z, pa.w, pb.x }, { pb.y, pb.z, pb.w } });
     }
   }
   cluster.sync(); // CTA 0 has read every CTA's pieces: the others may exit
@@ -1719,7 +1711,8 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   if (!merging)
     return;
   const uint32_t P = s_pre[C];
-  merge_walks([&](uint32_t i) { return m_box[2 * i]; }, n, P, 0u, -1, m_R, m_d, m_slot, m_box, m_out, &s_nout, st);
+  merge_walks([&](uint32_t i) { return load_box8(m_box + 2 * i); }, n, P, 0u, -1, m_R, m_d, m_slot, m_box, m_out, &s_nout,
+              st);
   __syncthreads();
   merge_write_out(n, P, 0u, -1, m_R, m_d, m_slot, m_box, nodes, m_out, &s_nout);
   __syncthreads();

@@ -169,7 +169,7 @@ constexpr size_t kSmMergeSlot = kSmMergeR + kSmallMergeCap * 4;
 constexpr size_t kSmMergeD = kSmMergeSlot + kSmallMergeCap * 4;
 constexpr size_t kSmMergeOut = kSmMergeD + kSmallMergeCap;
 constexpr size_t kSmMerge = kSmMergeOut + kMergeOut * 48;
-constexpr size_t kSmSort = 32 * 256 * 2 + 4 * 256 * 4; // uint16[32 warps][256 digits], uint32[4][256]
+constexpr size_t kSmSort = 32 * 1024 * 2; // uint16[32 warps][1024 digits]
 constexpr size_t kSmallSmem =
   kSmUnion + (kSmMerge > kSmTree ? (kSmMerge > kSmSort ? kSmMerge : kSmSort) : (kSmTree > kSmSort ? kSmTree : kSmSort));
 static_assert(kSmUnion % 32 == 0 && kSmPiece % 32 == 0 && kSmTreeRec % 32 == 0, "small build smem alignment");

@@ -164,13 +164,35 @@ load_node_box(const Node* __restrict__ nodes, uint32_t idx)
 __device__ __forceinline__ void
 stage_record(Node& rec, const Box& b, uint32_t l, uint32_t r)
 {
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    rec.lo[k] = b.lo[k];
-    rec.hi[k] = b.hi[k];
-  }
-  rec.left = l;
-  rec.right = r;
+  float4* p = reinterpret_cast<float4*>(&rec); // records are 32-byte aligned
+  p[0] = make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]);
+  p[1] = make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r));
+}
+
+// The box of a record staged by stage_record.
+__device__ __forceinline__ Box
+staged_box(const Node& rec)
+{
+  const float4 a = reinterpret_cast<const float4*>(&rec)[0];
+  const float2 b = reinterpret_cast<const float2*>(&rec)[2];
+  return Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
+}
+
+// A box at an 8-byte aligned address (arrays of Box), as three 8-byte accesses.
+__device__ __forceinline__ Box
+load_box8(const Box* p)
+{
+  const float2* q = reinterpret_cast<const float2*>(p);
+  const float2 a = q[0], b = q[1], c = q[2];
+  return Box{ { a.x, a.y, b.x }, { b.y, c.x, c.y } };
+}
+__device__ __forceinline__ void
+store_box8(Box* p, const Box& b)
+{
+  float2* q = reinterpret_cast<float2*>(p);
+  q[0] = make_float2(b.lo[0], b.lo[1]);
+  q[1] = make_float2(b.lo[2], b.hi[0]);
+  q[2] = make_float2(b.hi[1], b.hi[2]);
 }
 
 // Asynchronous 16-byte copy global -> shared (cp.async, L2 only); bytes
