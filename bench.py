@@ -706,7 +706,8 @@ def measure_config1(ctx, stream, flush, dev, steps):
             "value": round(m / ((b + tr) * 1e-3) / 1e6, 1), "unit": "Mrays/s", "ms_per_step": round(b + tr, 4),
             "build_ms": round(b, 4), "trace_ms": round(tr, 4),
             "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")},
-            "trace_tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill", "trace_blocks_per_sm")}}
+            "trace_tuning": {k: trace_tuning.get(k, 0) for k in ("trace_leaf_batch", "trace_refill", "trace_blocks_per_sm",
+                                                                 "trace_ray_order")}}
 
 
 def summary_line(line):
@@ -756,6 +757,8 @@ def main():
                     help="1: walk tree nodes crossing CTA edges from the local phase's tail (default: the library's)")
     ap.add_argument("--small-build-max", type=int, default=None,
                     help="largest build run as one cluster launch, 0 = never (default: the library's)")
+    ap.add_argument("--trace-ray-order", type=int, default=None,
+                    help="1: traverse the rays in sorted order (default: the tuner's choice)")
     ap.add_argument("--trace-refill", type=int, default=None,
                     help="idle lanes at which a traversal warp takes new rays (default: the library's)")
     ap.add_argument("--trace-blocks", type=int, default=None,
@@ -802,6 +805,8 @@ def main():
         ctx.set_param(_lib.PARAM_TRACE_BLOCKS_PER_SM, args.trace_blocks)
     if args.trace_leaf_batch is not None:
         ctx.set_param(_lib.PARAM_TRACE_LEAF_BATCH, args.trace_leaf_batch)
+    if args.trace_ray_order is not None:
+        ctx.set_param(_lib.PARAM_TRACE_RAY_ORDER, args.trace_ray_order)
     if args.tree_walk_fused is not None:
         ctx.set_param(_lib.PARAM_TREE_WALK_FUSED, args.tree_walk_fused)
     if args.small_build_max is not None:
@@ -849,9 +854,15 @@ def main():
     hits_b = torch.empty((bounce.shape[0], 4), dtype=torch.float32, device=dev)
     m = prim.shape[0] + bounce.shape[0]
     config = room_config(tris_h, prim_h, bounce_h, world)
-    # the traversal's leaf batching, refill and grid, tuned on the step's own rays
-    # (a sparse sample neither fills the GPU nor keeps the rays' coherence)
-    trace_tuning = autotune.tune_trace(ctx, bvh, torch.cat([prim, bounce]), key=f"gb300:trace:{WORKLOAD}")
+    # the traversal's leaf batching, refill, grid and ray order, tuned on the
+    # step's own two traces (a sparse sample neither fills the GPU nor keeps
+    # the rays' coherence)
+    trace_tuning = dict(autotune.tune_trace(ctx, bvh, [prim, bounce], key=f"gb300:trace:{WORKLOAD}"))
+    for flag, key in (("trace_refill", "trace_refill"), ("trace_blocks", "trace_blocks_per_sm"),
+                      ("trace_leaf_batch", "trace_leaf_batch"), ("trace_ray_order", "trace_ray_order")):
+        if getattr(args, flag) is not None:  # an explicit setting overrides the tuned one
+            trace_tuning[key] = getattr(args, flag)
+            autotune.apply(ctx, {key: trace_tuning[key]})
 
     for _ in range(args.warmup):
         builder(tris, into=bvh)
@@ -934,7 +945,8 @@ def main():
                   "tuning": {k: tuning[k] for k in ("sort_tile_keys", "bucket_sort_min", "bounds_blocks_per_sm")}},
         "trace": {"ms": round(trace_ms, 4), "mrays_s": round(m / (trace_ms * 1e-3) / 1e6, 1),
                   "primary_hit_fraction": round(hit_frac, 4),
-                  "tuning": {k: trace_tuning[k] for k in ("trace_leaf_batch", "trace_refill", "trace_blocks_per_sm")}},
+                  "tuning": {k: trace_tuning.get(k, 0) for k in ("trace_leaf_batch", "trace_refill", "trace_blocks_per_sm",
+                                                                  "trace_ray_order")}},
     }
     detail("build_tuning", tuning)
     detail("trace_tuning", trace_tuning)

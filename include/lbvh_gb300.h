@@ -151,6 +151,11 @@ LBVH_API int lbvh_ctx_reserve(lbvh_ctx* ctx, size_t n_prims, size_t n_rays);
                                             as one launch: a cluster of up to 16 CTAs that keeps the
                                             boxes, codes, sort and tree in shared memory; 0 always takes
                                             the multi-kernel build (the same nodes either way) */
+#define LBVH_PARAM_TRACE_RAY_ORDER 17  /* 1: a trace of at least 4,096 rays whose hits go to device memory
+                                            (or are staged there) first sorts the rays by origin cell, then
+                                            direction cell (4 bits per axis each), and traverses them in that
+                                            order; every hit still goes to its ray's slot, so the results
+                                            are the same; 0 (default): the caller's order */
 #define LBVH_PARAM_LOOKBACK_SPIN_LIMIT 6 /* polls of a radix-sort look-back wait before the build gives up
                                             and reports LBVH_ERR_TIMEOUT, 1..2^24 (default 2^22, a few
                                             seconds); no tree is built after a wait gave up */

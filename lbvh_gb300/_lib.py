@@ -43,6 +43,7 @@ PARAM_BOUNDS_BLOCKS_PER_SM = 13
 PARAM_TREE_WALK_FUSED = 14
 PARAM_TEST_TREE_MERGE_CAP = 15
 PARAM_SMALL_BUILD_MAX = 16
+PARAM_TRACE_RAY_ORDER = 17
 LBVH_BUILD_SORTED_LEAVES = 0x1
 LBVH_BUILD_KEEP_CURVE = 0x2
 LEAF_BIT = 0x80000000

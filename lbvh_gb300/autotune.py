@@ -58,6 +58,7 @@ _PARAMS = {
     "bucket_sort_min": "PARAM_BUCKET_SORT_MIN",
     "bounds_blocks_per_sm": "PARAM_BOUNDS_BLOCKS_PER_SM",
     "trace_in_place": "PARAM_TRACE_IN_PLACE",
+    "trace_ray_order": "PARAM_TRACE_RAY_ORDER",
 }
 
 
@@ -222,13 +223,14 @@ def tune_build(ctx, tris, reps: int = 5, table_path: str | None = None, force: b
 
 def tune_trace(ctx, bvh, rays, key: str, sample: int | None = None, reps: int = 2, table_path: str | None = None,
                force: bool = False) -> dict:
-    """Best leaf-test batching, refill threshold and grid for tracing `rays`
-    (a device [m, 8] array) against `bvh`; cached under `key`. Timed on all
-    the rays by default: a sample too small to fill the GPU, or too sparse
-    to keep neighbouring rays together, favours other settings than the
-    full workload does. `sample` times about that many rays instead, taken
-    as evenly spaced runs of 4,096 consecutive rays. Returns the setting and
-    applies it."""
+    """Best leaf-test batching, refill threshold, grid and ray order for
+    tracing `rays` (a device [m, 8] array, or a list of them traced one after
+    another, as a step that traces several ray sets does) against `bvh`;
+    cached under `key`. Timed on all the rays by default: a sample too small
+    to fill the GPU, or too sparse to keep neighbouring rays together,
+    favours other settings than the full workload does. `sample` (a single
+    array only) times about that many rays instead, taken as evenly spaced
+    runs of 4,096 consecutive rays. Returns the setting and applies it."""
     import torch
 
     from .api import Traverser
@@ -238,25 +240,30 @@ def tune_trace(ctx, bvh, rays, key: str, sample: int | None = None, reps: int = 
         apply(ctx, table[key])
         return table[key]
     stream = torch.cuda.current_stream()
-    m = int(rays.shape[0])
-    if sample is None or sample >= m:
-        part = rays
-    else:
+    sets = list(rays) if isinstance(rays, (list, tuple)) else [rays]
+    if len(sets) == 1 and sample is not None and sample < int(sets[0].shape[0]):
+        m = int(sets[0].shape[0])
         run = 4096
         starts = np.linspace(0, m - run, max(1, sample // run)).astype(np.int64) if m > run else np.zeros(1, np.int64)
-        part = torch.cat([rays[int(a):int(a) + run] for a in starts]).contiguous()
-    out = torch.empty((part.shape[0], 4), dtype=torch.float32, device=rays.device)
+        sets = [torch.cat([sets[0][int(a):int(a) + run] for a in starts]).contiguous()]
+    outs = [torch.empty((r.shape[0], 4), dtype=torch.float32, device=r.device) for r in sets]
     trav = Traverser(bvh)
     ms = {}
     for leaf in TRACE_LEAF_BATCH:
         for refill in TRACE_REFILL:
             for grid in TRACE_GRID if leaf > 1 else TRACE_GRID[:1]:
                 apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid})
-                ms[(leaf, refill, grid)] = _time(lambda: trav(part, out=out), stream, reps)
+                ms[(leaf, refill, grid)] = _time(lambda: [trav(r, out=o) for r, o in zip(sets, outs)], stream, reps)
     leaf, refill, grid = min(ms, key=ms.get)
+    # the same setting with the rays traversed in sorted order
+    apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid, "trace_ray_order": 1})
+    ordered = _time(lambda: [trav(r, out=o) for r, o in zip(sets, outs)], stream, reps)
+    ctx.set_param(_lib.PARAM_TRACE_RAY_ORDER, 0)
     setting = {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid,
-               "sample_rays": int(part.shape[0]),
-               "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in ms.items()}}
+               "trace_ray_order": int(ordered < ms[(leaf, refill, grid)]),
+               "sample_rays": int(sum(int(r.shape[0]) for r in sets)),
+               "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in ms.items()},
+               "trace_ms_ordered": round(ordered, 4)}
     _store(table, key, setting, table_path)
     apply(ctx, setting)
     return setting

@@ -47,6 +47,8 @@ struct lbvh_ctx
   DevBuf rays;                 // staging for host rays
   DevBuf hits;                 // staging for host hits
   DevBuf counts;               // staging for host per-ray counts
+  DevBuf ray_sort;             // ray order: keys and indices, two of each (16 B per ray)
+  uint32_t ray_order = 0;      // LBVH_PARAM_TRACE_RAY_ORDER
   DevBuf prims_in;             // staging for host refit input
   DevBuf roff;                 // staging for host batch ray offsets
   uint32_t* ray_counter = nullptr; // persistent-trace ray dispenser
@@ -268,6 +270,41 @@ next_epoch(lbvh_ctx* c, uint32_t* base)
   }
   *base = c->epoch;
   c->epoch += 4;
+  return LBVH_OK;
+}
+
+// The trace order of m device rays (LBVH_PARAM_TRACE_RAY_ORDER): their
+// sort keys (origin cell above direction cell), then the stable pairs sort
+// the builds use; *order gets the ray indices in key order.
+int
+order_rays(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, uint32_t m, const uint32_t** order)
+{
+  const size_t tiles = sort_tiles_any(m);
+  bool grew = false;
+  CK(reserve(c->lookback, tiles * 256 * 8, c->stream, &grew), "look-back allocation");
+  if (grew)
+    CK(cudaMemsetAsync(c->lookback.ptr, 0, c->lookback.cap, c->stream), "look-back clear");
+  CK(reserve(c->ray_sort, 16 * size_t(m), c->stream), "ray order allocation");
+  BuildBuffers rb = c->bufs;
+  uint32_t* base = static_cast<uint32_t*>(c->ray_sort.ptr);
+  rb.keys_a = base;
+  rb.keys_b = base + m;
+  rb.vals_a = base + 2 * size_t(m);
+  rb.vals_b = base + 3 * size_t(m);
+  rb.lookback = static_cast<unsigned long long*>(c->lookback.ptr);
+  rb.msd = false;
+  // the sort's digit histograms and tile dispensers start at zero (a build
+  // resets them itself)
+  CK(cudaMemsetAsync(&c->state->hist[0][0], 0, sizeof(c->state->hist) + sizeof(c->state->tile_counter), c->stream),
+     "ray order state reset");
+  uint32_t epoch;
+  int st = next_epoch(c, &epoch);
+  if (st)
+    return st;
+  CK(launch_ray_keys(rays, m, static_cast<const Node*>(b->nodes.ptr), rb.keys_a, c->state, c->stream),
+     "ray key launch");
+  CK(launch_sort(m, true, epoch, rb, c->stream), "ray sort launch");
+  *order = rb.vals_a;
   return LBVH_OK;
 }
 
@@ -734,6 +771,11 @@ lbvh_ctx_set_param(lbvh_ctx* c, int param, int value)
         return fail(c, LBVH_ERR_INVALID_ARG, "one-launch build limit %d outside [0, %u]", value, kSmallMaxPrims);
       c->small_max = uint32_t(value);
       return LBVH_OK;
+    case LBVH_PARAM_TRACE_RAY_ORDER:
+      if (value < 0 || value > 1)
+        return fail(c, LBVH_ERR_INVALID_ARG, "ray order %d is not 0 or 1", value);
+      c->ray_order = uint32_t(value);
+      return LBVH_OK;
     case LBVH_PARAM_TEST_TREE_MERGE_CAP:
       if (value < 0 || value > int(kMergeCap))
         return fail(c, LBVH_ERR_INVALID_ARG, "tree merge capacity %d outside [0, %u]", value, kMergeCap);
@@ -1089,9 +1131,12 @@ trace_common(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, size_t m, void* 
     }
     return check_device(c);
   }
+  const uint32_t* order = nullptr;
+  if (c->ray_order && !(hits_in_place && !counts) && m >= 4096 && (st = order_rays(c, b, dr, uint32_t(m), &order)))
+    return st;
   CK(launch_trace_tris(static_cast<const WideNode*>(b->wnodes.ptr), b->n - 1, tris, leaf_prim, dr, uint32_t(m), dh,
                        counts ? db : nullptr, counts ? dt : nullptr, c->ray_counter, c->num_sms, c->trace,
-                       c->stream, hits_in_place && !counts),
+                       c->stream, hits_in_place && !counts, order),
      "trace launch");
   if (hh)
     CK(cudaMemcpyAsync(hits, dh, 16 * m, cudaMemcpyDeviceToHost, c->stream), "hit download");

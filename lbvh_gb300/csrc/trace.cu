@@ -261,6 +261,7 @@ k_trace(const WideNode* __restrict__ wnodes,
         const uint32_t* __restrict__ wide,
         uint32_t refill,
         uint32_t leaf_batch,
+        const uint32_t* __restrict__ order,
         const uint32_t* __restrict__ moff,
         const uint32_t* __restrict__ roff,
         uint32_t n_meshes)
@@ -380,6 +381,8 @@ k_trace(const WideNode* __restrict__ wnodes,
             id_buf = batch_buf;
           }
           if (id < m) {
+            if (order) // rays taken in a sorted order; each hit still goes to its ray's slot
+              id = __ldg(order + id);
             ray = id;
             if (kHostHits)
               buf = id_buf;
@@ -537,6 +540,70 @@ k_trace(const WideNode* __restrict__ wnodes,
   }
 }
 
+// Ray sort keys (launch_ray_keys): a heuristic trace order, so any key is
+// correct; the traversal of each ray and its hit do not depend on it.
+__device__ __forceinline__ uint32_t
+cell4(float v, float lo, float inv)
+{
+  const float q = (v - lo) * inv; // NaN and out-of-range values clamp
+  return q >= 15.0f ? 15u : (q > 0.0f ? uint32_t(q) : 0u);
+}
+
+__device__ __forceinline__ uint32_t
+spread4(uint32_t x) // 4 bits to every third bit
+{
+  return (x & 1u) | ((x & 2u) << 2) | ((x & 4u) << 4) | ((x & 8u) << 6);
+}
+
+__global__ __launch_bounds__(256) void
+k_ray_keys(const float4* __restrict__ rays, uint32_t m, const Node* __restrict__ nodes, uint32_t* __restrict__ keys,
+           BuildState* __restrict__ st)
+{
+  __shared__ uint32_t s_hist[3 * 256];
+  for (uint32_t k = threadIdx.x; k < 3 * 256; k += blockDim.x)
+    s_hist[k] = 0;
+  __syncthreads();
+  const Node root = nodes[0];
+  float ilo[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float ext = root.hi[k] - root.lo[k];
+    ilo[k] = ext > 0.0f ? 16.0f / ext : 0.0f;
+  }
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const float4 a = __ldg(rays + 2 * size_t(i)), b = __ldg(rays + 2 * size_t(i) + 1);
+    const float dx = a.w, dy = b.x, dz = b.y;
+    const float big = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+    const float id = big > 0.0f ? 8.0f / big : 0.0f; // components to [-8, 8], then cells of 1
+    const uint32_t o = (spread4(cell4(a.x, root.lo[0], ilo[0])) << 2) | (spread4(cell4(a.y, root.lo[1], ilo[1])) << 1) |
+                       spread4(cell4(a.z, root.lo[2], ilo[2]));
+    const uint32_t d = (spread4(cell4(dx * id, -8.0f, 1.0f)) << 2) | (spread4(cell4(dy * id, -8.0f, 1.0f)) << 1) |
+                       spread4(cell4(dz * id, -8.0f, 1.0f));
+    const uint32_t key = (o << 12) | d;
+    keys[i] = key;
+    atomicAdd(&s_hist[key & 255u], 1u);
+    atomicAdd(&s_hist[256 + ((key >> 8) & 255u)], 1u);
+    atomicAdd(&s_hist[512 + (key >> 16)], 1u);
+  }
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < 3 * 256; k += blockDim.x)
+    if (s_hist[k])
+      atomicAdd(&(&st->hist[0][0])[k], s_hist[k]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) // the fourth digit is zero for every key
+    atomicAdd(&st->hist[3][0], m);
+}
+
+cudaError_t
+launch_ray_keys(const float* rays, uint32_t m, const Node* nodes, uint32_t* keys, BuildState* st, cudaStream_t s)
+{
+  int dev = 0, sms = 1;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint32_t want = ceil_div_u32(m, 256), cap = uint32_t(sms) * 8;
+  k_ray_keys<<<want < cap ? want : cap, 256, 0, s>>>(reinterpret_cast<const float4*>(rays), m, nodes, keys, st);
+  return cudaGetLastError();
+}
+
 cudaError_t
 launch_repack(const Node* nodes, uint32_t n_nodes, WideNode* out, cudaStream_t s)
 {
@@ -563,7 +630,8 @@ launch_trace_tris(const WideNode* wnodes,
                   int num_sms,
                   const TraceParams& p,
                   cudaStream_t s,
-                  bool host_hits)
+                  bool host_hits,
+                  const uint32_t* order)
 {
   if (m == 0)
     return cudaSuccess;
@@ -579,7 +647,7 @@ launch_trace_tris(const WideNode* wnodes,
   // leaf batching pays for long rays in loose trees (the tuner decides)
   auto go = [&](auto kernel, uint32_t* nb, uint32_t* nt) {
     kernel<<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nb, nt, ray_counter, wide, p.refill,
-                                           p.leaf_batch, nullptr, nullptr, 0);
+                                           p.leaf_batch, host_hits ? nullptr : order, nullptr, nullptr, 0);
   };
   const bool counts = n_box && n_tri;
   if (p.leaf_batch > 1) {
@@ -825,11 +893,11 @@ launch_batch_trace(const WideNode* wnodes,
   if (p.leaf_batch > 1)
     k_trace<false, true, false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr,
                                                                       nullptr, ray_counter, wide, p.refill,
-                                                                      p.leaf_batch, off, roff, n_meshes);
+                                                                      p.leaf_batch, nullptr, off, roff, n_meshes);
   else
     k_trace<false, true><<<blocks, kTraceThreads, 0, s>>>(wnodes, tris, leaf_prim, r4, m, hits, nullptr, nullptr,
-                                                          ray_counter, wide, p.refill, p.leaf_batch, off, roff,
-                                                          n_meshes);
+                                                          ray_counter, wide, p.refill, p.leaf_batch, nullptr, off,
+                                                          roff, n_meshes);
   return cudaGetLastError();
 }
 

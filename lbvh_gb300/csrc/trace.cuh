@@ -42,7 +42,16 @@ cudaError_t launch_trace_tris(const WideNode* wnodes,
                               int num_sms,
                               const TraceParams& p,
                               cudaStream_t s,
-                              bool host_hits = false); // hits: page-locked host memory
+                              bool host_hits = false,         // hits: page-locked host memory
+                              const uint32_t* order = nullptr); // device hits only: trace ray order[q] q-th
+
+// Sort keys of m rays for a coherent trace order: the origin's cell (4 bits
+// per axis of the root box, z-order) above the direction's cell (4 bits per
+// axis of the direction scaled by its largest component), 24 bits; the key
+// histograms of the sort's four 8-bit digits go to st->hist, which must be
+// zero.
+cudaError_t launch_ray_keys(const float* rays, uint32_t m, const Node* nodes, uint32_t* keys, BuildState* st,
+                            cudaStream_t s);
 
 // Hit record of the sphere intersector: {prim, t, uv, normal, pad}, 32 bytes.
 struct __align__(16) SphereHit

@@ -263,3 +263,39 @@ def test_leaf_batch_settings_match(ctx, port, leaf_batch):
     assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
     with pytest.raises(ValueError):
         c.set_param(_lib.PARAM_TRACE_LEAF_BATCH, 0)
+
+
+@pytest.mark.parametrize("leaf_batch", [1, 8])
+def test_sorted_ray_order_gives_the_same_hits(ctx, port, leaf_batch):
+    """With LBVH_PARAM_TRACE_RAY_ORDER the rays are traversed in sorted order
+    (origin cell, then direction cell), and every hit and per-ray count
+    still lands in its ray's slot: the reference's hits for the room's
+    primary and diffuse bounce rays (device, host and page-locked buffers),
+    the torus config's incoherent rays, and sizes on either side of the
+    4,096-ray minimum."""
+    c = lb.Context()
+    c.set_param(_lib.PARAM_TRACE_LEAF_BATCH, leaf_batch)
+    c.set_param(_lib.PARAM_TRACE_RAY_ORDER, 1)
+    room = scenes.room_scene(seed=21)
+    nodes = port.build(room, 16)
+    prim = np.ascontiguousarray(scenes.pinhole_rays(1920, 1080, eye=(0.0, 3.0, 9.0), target=(0.0, 2.0, 0.0))[::23])
+    bvh = lb.Builder(c)(dev(room))
+    trav = lb.Traverser(bvh)
+    want_p, nb, nt = port.trace(nodes, room, prim, 16, counts=True)
+    assert_hits_equal(lb.hits_view(trav(dev(prim))), want_p)
+    got, gb, gt = trav(prim, counts=True)
+    assert_hits_equal(got, want_p)
+    assert np.array_equal(gb, nb) and np.array_equal(gt, nt)
+    bounce = scenes.diffuse_bounce(prim, want_p, room, seed=22)
+    want_b = port.trace(nodes, room, bounce, 16)
+    assert_hits_equal(lb.hits_view(trav(dev(bounce))), want_b)
+    assert_hits_equal(trav(bounce), want_b)  # host rays and hits
+    pinned = torch.from_numpy(bounce).pin_memory()
+    assert_hits_equal(lb.hits_view(trav(pinned)), want_b)
+    for m in (4095, 4096, 4097, 9999):
+        assert_hits_equal(lb.hits_view(trav(dev(bounce[:m]))), want_b[:m])
+    t = scenes.torus_scene(seed=11)
+    rays = scenes.incoherent_rays(t, 1 << 16, 3)
+    assert_hits_equal(lb.hits_view(lb.Traverser(lb.Builder(c)(dev(t)))(dev(rays))), port.trace(port.build(t, 8), t, rays, 16))
+    with pytest.raises(ValueError):
+        c.set_param(_lib.PARAM_TRACE_RAY_ORDER, 2)
