@@ -656,6 +656,31 @@ def ctx_in_place(ctx, transfer, args):
     return args.e2e_in_place if args.e2e_in_place is not None else transfer["trace_in_place"]
 
 
+def build_launches(n, tuning):
+    """Kernel launches of one keys-only build of n primitives: one cluster
+    launch up to 16,384; else bounds, Morton codes, the bucket sort's three
+    kernels when it runs, the four onesweep passes, the local tree phase and
+    the merge levels (as the library lays them out)."""
+    if n <= 16384:
+        return 1
+    groups, merges, level = -(-n // 1024), 0, 0
+    while groups > 1:
+        window = groups if groups <= (160 if level == 0 else 96) else 128
+        groups = -(-groups // window)
+        merges += 1
+        level += 1
+    bucket = n >= int(tuning.get("bucket_sort_min", 1_500_000))
+    return 2 + (3 if bucket else 0) + 4 + 1 + merges
+
+
+def step_launches(n, tuning, trace_tuning, traces=2):
+    """Kernel launches of one bench step: the build, the traversal copy
+    (k_repack) and each trace (with the ray order: the key kernel and three
+    sort passes before it)."""
+    per_trace = 1 + (4 if trace_tuning.get("trace_ray_order") else 0)
+    return build_launches(n, tuning) + 1 + traces * per_trace
+
+
 def time_steps(builder, bvh, trav, tris, ray_sets, hit_sets, flush, stream, steps):
     """K whole steps (build, then one trace per ray set) timed with CUDA
     events on the launching stream, L2 flushed before each step. Returns
@@ -886,9 +911,7 @@ def main():
     build_ms = float(np.mean([x for x, _ in t]))
     trace_ms = float(np.mean([y for _, y in t]))
     step_ms, value = replica_throughput(build_ms + trace_ms, m, world, dev)
-    # per step: bounds, Morton, four onesweep passes, local + global tree
-    # phases; the traversal copy (k_repack); two traversals
-    gpu_launches = args.steps * (8 + 1 + 2)
+    gpu_launches = args.steps * step_launches(n, tuning, trace_tuning)
 
     # correctness guard on the timed output: the same hits as a fresh build
     ref_p = torch.empty_like(hits_p)

@@ -303,8 +303,8 @@ order_rays(lbvh_ctx* c, const lbvh_bvh* b, const float* rays, uint32_t m, const 
     return st;
   CK(launch_ray_keys(rays, m, static_cast<const Node*>(b->nodes.ptr), rb.keys_a, c->state, c->stream),
      "ray key launch");
-  CK(launch_sort(m, true, epoch, rb, c->stream), "ray sort launch");
-  *order = rb.vals_a;
+  CK(launch_sort(m, true, epoch, rb, c->stream, 3), "ray sort launch"); // 24-bit keys: three passes
+  *order = rb.vals_b;
   return LBVH_OK;
 }
 

@@ -1910,7 +1910,7 @@ launch_curve(const Leaf& leaf, uint32_t n, const BuildBuffers& b, cudaStream_t s
 }
 
 cudaError_t
-launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s)
+launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s, uint32_t passes)
 {
   const bool msd = b.msd && !pairs;
   if (msd) {
@@ -1945,7 +1945,7 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
   uint32_t* vb = b.vals_b;
   const uint32_t spin = b.spin_limit ? b.spin_limit : kSpinLimit;
   const uint32_t wx = b.wait_xor;
-  for (uint32_t pass = 0; pass < 4; pass++) {
+  for (uint32_t pass = 0; pass < passes; pass++) {
     const uint32_t epoch = epoch_base + pass;
     if (pairs) {
       if (pass == 0)
@@ -1964,7 +1964,7 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
     std::swap(ka, kb);
     std::swap(va, vb);
   }
-  // four passes: sorted keys (and values) are back in keys_a / vals_a
+  // an even pass count leaves the sorted keys (and values) in keys_a / vals_a
   return cudaGetLastError();
 }
 

@@ -242,7 +242,10 @@ cudaError_t launch_small_build_boxes(const Box* boxes, uint32_t n, uint32_t* cod
 // leaf instead of the 48-byte triangle.
 cudaError_t launch_curve_tris(const Tri* tris, uint32_t n, const BuildBuffers& b, cudaStream_t s);
 cudaError_t launch_curve_boxes(const Box* boxes, uint32_t n, const BuildBuffers& b, cudaStream_t s);
-cudaError_t launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s);
+// passes < 4 (keys below 2^(8 passes)): the sorted keys / values end in
+// keys_b / vals_b when passes is odd, else in keys_a / vals_a.
+cudaError_t launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, cudaStream_t s,
+                        uint32_t passes = 4);
 // Tree construction + box fit from the sorted codes in keys_a; `epoch` tags
 // this build's arrival slots and must differ from every earlier one on the
 // same slots.

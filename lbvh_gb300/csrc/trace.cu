@@ -570,8 +570,15 @@ k_ray_keys(const float4* __restrict__ rays, uint32_t m, const Node* __restrict__
     const float ext = root.hi[k] - root.lo[k];
     ilo[k] = ext > 0.0f ? 16.0f / ext : 0.0f;
   }
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    const float4 a = __ldg(rays + 2 * size_t(i)), b = __ldg(rays + 2 * size_t(i) + 1);
+  const uint32_t lane = threadIdx.x & 31;
+  // whole warps iterate together, so the digit counts can be added once per
+  // warp and value (a digit that most rays share -- the origin cell of
+  // camera rays -- would otherwise serialize its shared-memory atomics)
+  for (uint32_t base = blockIdx.x * blockDim.x; base < m; base += gridDim.x * blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const bool valid = i < m;
+    const float4 a = valid ? __ldg(rays + 2 * size_t(i)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 b = valid ? __ldg(rays + 2 * size_t(i) + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float dx = a.w, dy = b.x, dz = b.y;
     const float big = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
     const float id = big > 0.0f ? 8.0f / big : 0.0f; // components to [-8, 8], then cells of 1
@@ -580,10 +587,15 @@ k_ray_keys(const float4* __restrict__ rays, uint32_t m, const Node* __restrict__
     const uint32_t d = (spread4(cell4(dx * id, -8.0f, 1.0f)) << 2) | (spread4(cell4(dy * id, -8.0f, 1.0f)) << 1) |
                        spread4(cell4(dz * id, -8.0f, 1.0f));
     const uint32_t key = (o << 12) | d;
-    keys[i] = key;
-    atomicAdd(&s_hist[key & 255u], 1u);
-    atomicAdd(&s_hist[256 + ((key >> 8) & 255u)], 1u);
-    atomicAdd(&s_hist[512 + (key >> 16)], 1u);
+    if (valid)
+      keys[i] = key;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const uint32_t dg = valid ? (key >> (8 * k)) & 255u : 256u + lane; // invalid lanes match nobody
+      const uint32_t peers = __match_any_sync(0xffffffffu, dg);
+      if (valid && (__ffs(peers) - 1) == int(lane))
+        atomicAdd(&s_hist[256 * k + dg], uint32_t(__popc(peers)));
+    }
   }
   __syncthreads();
   for (uint32_t k = threadIdx.x; k < 3 * 256; k += blockDim.x)
