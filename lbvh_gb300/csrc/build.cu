@@ -1150,9 +1150,9 @@ k_tree_local(Leaf leaf,
   __syncthreads();
   const uint32_t np = s_npend;
   if (walk_on) {
-    // The global phase starts here: each pending node walks up through the
-    // global arrival slots at once, so chains across CTA edges overlap the
-    // local phases of the CTAs still to run. This CTA's records were all
+    // The walks above this CTA's pieces start here: each piece walks up
+    // through the global arrival slots at once, so chains across CTA edges
+    // overlap the local phases of the CTAs still to run. This CTA's records were all
     // written before the barrier above; the fence orders them before the
     // walk's first release.
     if (tid == 0 && np > kTreePendingPerBlock)
