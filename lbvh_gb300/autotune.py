@@ -41,6 +41,7 @@ TRACE_BLOCKS_PER_SM = (6, 8)
 TRACE_REFILL = (8, 12, 16)
 TRACE_LEAF_BATCH = (1, 4, 8)
 TRACE_GRID = (8, 9)  # CTAs per SM; the leaf-batching variant is compiled to fit 9
+TRACE_RAY_ORDER = (0, 1)  # the caller's order, sorted by origin and direction cells
 SORT_TILE_KEYS = (1024, 4096)
 BOUNDS_BLOCKS_PER_SM = (2, 4, 8)
 BUCKET_SORT_MIN = 65536  # the smallest size the bucket sort may take
@@ -249,21 +250,18 @@ def tune_trace(ctx, bvh, rays, key: str, sample: int | None = None, reps: int = 
     outs = [torch.empty((r.shape[0], 4), dtype=torch.float32, device=r.device) for r in sets]
     trav = Traverser(bvh)
     ms = {}
-    for leaf in TRACE_LEAF_BATCH:
-        for refill in TRACE_REFILL:
-            for grid in TRACE_GRID if leaf > 1 else TRACE_GRID[:1]:
-                apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid})
-                ms[(leaf, refill, grid)] = _time(lambda: [trav(r, out=o) for r, o in zip(sets, outs)], stream, reps)
-    leaf, refill, grid = min(ms, key=ms.get)
-    # the same setting with the rays traversed in sorted order
-    apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid, "trace_ray_order": 1})
-    ordered = _time(lambda: [trav(r, out=o) for r, o in zip(sets, outs)], stream, reps)
-    ctx.set_param(_lib.PARAM_TRACE_RAY_ORDER, 0)
+    for order in TRACE_RAY_ORDER:
+        for leaf in TRACE_LEAF_BATCH:
+            for refill in TRACE_REFILL:
+                for grid in TRACE_GRID if leaf > 1 else TRACE_GRID[:1]:
+                    apply(ctx, {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid,
+                                "trace_ray_order": order})
+                    ms[(leaf, refill, grid, order)] = _time(lambda: [trav(r, out=o) for r, o in zip(sets, outs)],
+                                                            stream, reps)
+    leaf, refill, grid, order = min(ms, key=ms.get)
     setting = {"trace_leaf_batch": leaf, "trace_refill": refill, "trace_blocks_per_sm": grid,
-               "trace_ray_order": int(ordered < ms[(leaf, refill, grid)]),
-               "sample_rays": int(sum(int(r.shape[0]) for r in sets)),
-               "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in ms.items()},
-               "trace_ms_ordered": round(ordered, 4)}
+               "trace_ray_order": order, "sample_rays": int(sum(int(r.shape[0]) for r in sets)),
+               "trace_ms": {"x".join(map(str, k)): round(v, 4) for k, v in ms.items()}}
     _store(table, key, setting, table_path)
     apply(ctx, setting)
     return setting

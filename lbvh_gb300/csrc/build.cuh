@@ -87,7 +87,8 @@ struct PieceHdr
 static_assert(sizeof(PieceHdr) == 16, "piece header layout");
 constexpr int kMergeThreads = 1024;
 constexpr uint32_t kMergeCap = 3200;        // pieces a merge CTA holds in shared memory
-constexpr uint32_t kMergeGroups = 128;      // groups per window below the last level
+constexpr uint32_t kMergeGroups = 128;      // local-phase groups per window below the last level
+constexpr uint32_t kMergeGroupsLater = 128; // window groups per window below the last level
 constexpr uint32_t kMergeFinalFirst = 160;  // local-phase groups the last level takes at once
 constexpr uint32_t kMergeFinalLater = 96;   // window groups the last level takes at once
 constexpr uint32_t kMergeMaxGroups = 160;   // largest window
@@ -132,7 +133,7 @@ tree_scratch(size_t n)
     if (g <= 1 || lv == kMergeMaxLevels)
       break;
     const uint32_t final_max = lv == 0 ? kMergeFinalFirst : kMergeFinalLater;
-    const uint32_t w = g <= final_max ? g : kMergeGroups;
+    const uint32_t w = g <= final_max ? g : (lv == 0 ? kMergeGroups : kMergeGroupsLater);
     t.window[lv] = w;
     t.merges = lv + 1;
     g = (g + w - 1) / w;
