@@ -665,7 +665,7 @@ def build_launches(n, tuning):
         return 1
     groups, merges, level = -(-n // 1024), 0, 0
     while groups > 1:
-        window = groups if groups <= (160 if level == 0 else 96) else 128
+        window = groups if groups <= (160 if level == 0 else 16) else (128 if level == 0 else 16)
         groups = -(-groups // window)
         merges += 1
         level += 1

@@ -1132,6 +1132,8 @@ k_tree_local(Leaf leaf,
   // boundaries k = b0 - 1 .. b0 + kTreeBlock - 1 at s_delta[k - (b0 - 1)]
   for (uint32_t j = tid; j <= kTreeBlock; j += kTreeThreads)
     s_delta[j] = boundary_delta(codes, n, b0 - 1 + j);
+  // the walks' first leaf-box loads wait on DRAM otherwise: start them now
+  leaf.prefetch(b0, count);
   for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
     s_slot[j] = kSlotEmpty;
     s_rec[j].left = 0; // no record (node 0, the root, is never a child)

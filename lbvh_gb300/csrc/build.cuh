@@ -88,11 +88,11 @@ static_assert(sizeof(PieceHdr) == 16, "piece header layout");
 constexpr int kMergeThreads = 1024;
 constexpr uint32_t kMergeCap = 3200;        // pieces a merge CTA holds in shared memory
 constexpr uint32_t kMergeGroups = 128;      // local-phase groups per window below the last level
-constexpr uint32_t kMergeGroupsLater = 128; // window groups per window below the last level
+constexpr uint32_t kMergeGroupsLater = 16;  // window groups per window below the last level
 constexpr uint32_t kMergeFinalFirst = 160;  // local-phase groups the last level takes at once
-constexpr uint32_t kMergeFinalLater = 96;   // window groups the last level takes at once
+constexpr uint32_t kMergeFinalLater = 16;   // window groups the last level takes at once
 constexpr uint32_t kMergeMaxGroups = 160;   // largest window
-constexpr uint32_t kMergeMaxLevels = 4;     // 2^30 leaves: 2^20 CTAs -> 8192 -> 64 -> 1
+constexpr uint32_t kMergeMaxLevels = 6;     // 2^30 leaves: 2^20 CTAs -> 8192 -> 512 -> 32 -> 2 -> 1
 constexpr uint32_t kMergeOut = kTreePendingPerBlock; // pieces a window leaves (two per tree level)
 // shared memory of k_tree_merge: group prefix, piece ends, deltas, slots,
 // two child boxes per slot, the window's own pieces
@@ -141,6 +141,9 @@ tree_scratch(size_t n)
   t.bytes = off;
   return t;
 }
+// the largest build still ends in one window
+static_assert(tree_scratch(kMaxPrims).groups[tree_scratch(kMaxPrims).merges] == 1,
+              "merge levels");
 
 // Keys-only builds of up to kSmallMaxPrims primitives run as one launch of
 // k_small_build: a thread-block cluster of ceil(n / kSmallSlots) CTAs, each
@@ -180,6 +183,14 @@ struct TriLeaf
 {
   const Tri* tris;
   __device__ __forceinline__ Box operator()(uint32_t i) const { return load_tri_box(tris, i); }
+  // Starts moving triangles [b0, b0 + cnt) into L2 (by the CTA's threads).
+  __device__ __forceinline__ void prefetch(uint32_t b0, uint32_t cnt) const
+  {
+    const char* p = reinterpret_cast<const char*>(tris + b0);
+    const uint32_t lines = (cnt * 48 + 127) / 128;
+    for (uint32_t k = threadIdx.x; k < lines; k += blockDim.x)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 128 * size_t(k)));
+  }
 };
 
 struct BoxLeaf
@@ -190,6 +201,14 @@ struct BoxLeaf
     const float2* p = reinterpret_cast<const float2*>(boxes + i);
     const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
     return Box{ { a.x, a.y, b.x }, { b.y, c.x, c.y } };
+  }
+  // Starts moving the boxes of leaves [b0, b0 + cnt) into L2 (by the CTA's threads).
+  __device__ __forceinline__ void prefetch(uint32_t b0, uint32_t cnt) const
+  {
+    const char* p = reinterpret_cast<const char*>(boxes + b0);
+    const uint32_t lines = (cnt * 24 + 127) / 128;
+    for (uint32_t k = threadIdx.x; k < lines; k += blockDim.x)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 128 * size_t(k)));
   }
 };
 
