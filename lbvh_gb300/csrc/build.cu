@@ -1029,7 +1029,7 @@ local_walks(const Leaf& leaf, uint32_t n, uint32_t b0, uint32_t count, const int
     const bool is_left = s_delta[R - b0 + 1] > s_delta[L - b0]; // delta(R) vs delta(L - 1)
     const uint32_t s = is_left ? R : L - 1;
     if (internal)
-      stage_record(s_rec[(is_left ? R : L) - b0], box, lref, rref);
+      stage_record_at(s_rec, (is_left ? R : L) - b0, box, lref, rref);
     if (s < b0 || s + 1 >= b0 + kSlots) { // split on the CTA's edge
       const uint32_t k = atomicAdd(s_npend, 1u);
       if (k < kTreePendingPerBlock)
@@ -1053,7 +1053,7 @@ local_walks(const Leaf& leaf, uint32_t n, uint32_t b0, uint32_t count, const int
     if (sib & kLeafBit) {
       other = leaf(sib & ~kLeafBit);
     } else {
-      other = staged_box(s_rec[sib - b0]);
+      other = staged_box_at(s_rec, sib - b0);
     }
     box = is_left ? join(box, other) : join(other, box);
     L = LP;
@@ -1062,7 +1062,7 @@ local_walks(const Leaf& leaf, uint32_t n, uint32_t b0, uint32_t count, const int
     rref = cr;
     internal = true;
     if (L == 0 && R == n - 1) { // the root: the whole tree fits in this CTA
-      stage_record(s_rec[0], box, lref, rref);
+      stage_record_at(s_rec, 0, box, lref, rref);
       active = false;
     }
   }
@@ -1077,10 +1077,10 @@ local_write_out(const Leaf& leaf, uint32_t n, uint32_t b0, Node* __restrict__ no
                 const Node* s_rec, PendingNode* s_pend, uint32_t* s_npend)
 {
   for (uint32_t j = threadIdx.x; j < kSlots; j += blockDim.x) {
-    const Node rec = s_rec[j];
-    if (rec.left != 0 && b0 + j + 1 < n)
-      store_node(nodes, b0 + j, Box{ { rec.lo[0], rec.lo[1], rec.lo[2] }, { rec.hi[0], rec.hi[1], rec.hi[2] } },
-                 rec.left, rec.right);
+    const float4 ra = *rec_half(s_rec, j, 0), rb = *rec_half(s_rec, j, 1);
+    const uint32_t rl = __float_as_uint(rb.z), rr = __float_as_uint(rb.w);
+    if (rl != 0 && b0 + j + 1 < n)
+      store_node(nodes, b0 + j, Box{ { ra.x, ra.y, ra.z }, { ra.w, rb.x, rb.y } }, rl, rr);
     const uint32_t v = s_slot[j];
     if (v != kSlotEmpty && v != kSlotComplete) {
       const uint32_t sj = b0 + j;
@@ -1090,8 +1090,7 @@ local_write_out(const Leaf& leaf, uint32_t n, uint32_t b0, Node* __restrict__ no
       if (wl == wr) {
         wb = leaf(wl);
       } else {
-        const Node& o = s_rec[(v <= sj ? wr : wl) - b0];
-        wb = Box{ { o.lo[0], o.lo[1], o.lo[2] }, { o.hi[0], o.hi[1], o.hi[2] } };
+        wb = staged_box_at(s_rec, (v <= sj ? wr : wl) - b0);
       }
       const uint32_t k = atomicAdd(s_npend, 1u);
       if (k < kTreePendingPerBlock)
@@ -1136,7 +1135,7 @@ k_tree_local(Leaf leaf,
   leaf.prefetch(b0, count);
   for (uint32_t j = tid; j < kTreeBlock; j += kTreeThreads) {
     s_slot[j] = kSlotEmpty;
-    s_rec[j].left = 0; // no record (node 0, the root, is never a child)
+    *staged_left_at(s_rec, j) = 0.0f; // no record (node 0, the root, is never a child)
   }
   if (tid == 0) {
     s_next = 0;
@@ -1642,7 +1641,7 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
       s_delta[j] = dv;
     }
     s_slot[tid] = kSlotEmpty;
-    s_rec[tid].left = 0; // no record (node 0, the root, is never a child)
+    *staged_left_at(s_rec, tid) = 0.0f; // no record (node 0, the root, is never a child)
     if (tid == 0) {
       s_next = 0;
       s_npend = 0;

@@ -161,21 +161,39 @@ load_node_box(const Node* __restrict__ nodes, uint32_t idx)
   return Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
 }
 
-__device__ __forceinline__ void
-stage_record(Node& rec, const Box& b, uint32_t l, uint32_t r)
+// Node records of the local tree phase in shared memory, 32 bytes each, with
+// the two 16-byte halves of record j swapped when bit 2 of j is set: a warp
+// touching records at random positions then spreads its 16-byte accesses
+// over all eight 16-byte bank groups, not the four that (2 j + half) mod 8
+// reaches otherwise.
+__device__ __forceinline__ float4*
+rec_half(Node* recs, uint32_t j, uint32_t half)
 {
-  float4* p = reinterpret_cast<float4*>(&rec); // records are 32-byte aligned
-  p[0] = make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]);
-  p[1] = make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r));
+  return reinterpret_cast<float4*>(recs + j) + (half ^ ((j >> 2) & 1u));
 }
-
-// The box of a record staged by stage_record.
-__device__ __forceinline__ Box
-staged_box(const Node& rec)
+__device__ __forceinline__ const float4*
+rec_half(const Node* recs, uint32_t j, uint32_t half)
 {
-  const float4 a = reinterpret_cast<const float4*>(&rec)[0];
-  const float2 b = reinterpret_cast<const float2*>(&rec)[2];
+  return reinterpret_cast<const float4*>(recs + j) + (half ^ ((j >> 2) & 1u));
+}
+__device__ __forceinline__ void
+stage_record_at(Node* recs, uint32_t j, const Box& b, uint32_t l, uint32_t r)
+{
+  *rec_half(recs, j, 0) = make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]);
+  *rec_half(recs, j, 1) = make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r));
+}
+__device__ __forceinline__ Box
+staged_box_at(const Node* recs, uint32_t j)
+{
+  const float4 a = *rec_half(recs, j, 0);
+  const float2 b = *reinterpret_cast<const float2*>(rec_half(recs, j, 1));
   return Box{ { a.x, a.y, a.z }, { a.w, b.x, b.y } };
+}
+// The left-child word of record j (0: no record staged there).
+__device__ __forceinline__ float*
+staged_left_at(Node* recs, uint32_t j)
+{
+  return &rec_half(recs, j, 1)->z;
 }
 
 // A box at an 8-byte aligned address (arrays of Box), as three 8-byte accesses.
