@@ -65,6 +65,34 @@ def test_noalloc_without_status_word(lib_built, port):
         assert nodes.cpu().numpy().view(lb.NODE_DTYPE).tobytes() == port.build(tris_h, 8).tobytes(), seed
 
 
+def test_noalloc_replays_in_a_captured_graph(lib_built, port):
+    """One call captured into a CUDA graph and replayed on new triangles in
+    the same buffer gives each soup's nodes: every replay clears the scratch
+    words it reads, so nothing of an earlier replay is taken as current."""
+    dev = torch.device("cuda", 0)
+    n = _lib.NOALLOC_MAX_PRIMS
+    tris = torch.from_numpy(scenes.soup(n, 80)).to(dev)
+    nodes = torch.empty(((n - 1) * 8,), dtype=torch.int32, device=dev)
+    status = torch.zeros((1,), dtype=torch.int32, device=dev)
+    s = torch.cuda.Stream(dev)
+    torch.cuda.synchronize()
+    assert _noalloc(tris, nodes, status, s.cuda_stream) == _lib.LBVH_OK  # the device's set-up, outside the capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+        rc = _noalloc(tris, nodes, status, s.cuda_stream)
+    assert rc == _lib.LBVH_OK
+    for seed in (81, 82):
+        t = scenes.soup(n, seed)
+        tris.copy_(torch.from_numpy(t))
+        status.fill_(0xFFFF)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        assert int(status.item()) == 0
+        assert nodes.cpu().numpy().view(lb.NODE_DTYPE).tobytes() == port.build(t, 8).tobytes(), seed
+
+
 def test_noalloc_rejects_what_it_cannot_serve(lib_built):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev).cuda_stream
