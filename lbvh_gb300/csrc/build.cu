@@ -274,7 +274,8 @@ k_onesweep(const uint32_t* __restrict__ kin,
            BuildState* __restrict__ st,
            bool skip_if_msd,
            uint32_t spin_limit,
-           uint32_t wait_xor)
+           uint32_t wait_xor,
+           uint32_t tiles)
 {
   pdl_begin(); // the predecessor in the stream has finished
   constexpr int kTile = kSortThreads * kItems;
@@ -289,12 +290,20 @@ k_onesweep(const uint32_t* __restrict__ kin,
   __shared__ uint32_t s_tile;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // A grid smaller than the tile count (the fallback passes of a bucket
+  // sort, which usually return at once) takes tiles until none is left;
+  // tiles are dispensed in order, so every look-back waits only on tiles
+  // that running CTAs hold.
+  const bool looping = gridDim.x < tiles;
+  for (;;) {
   if (tid == 0)
     s_tile = atomicAdd(&st->tile_counter[pass], 1u);
   for (int i = tid; i < kSortWarps * 256; i += kSortThreads)
     (&s_whist[0][0])[i] = 0;
   __syncthreads();
   const uint32_t tile = s_tile;
+  if (tile >= tiles)
+    break; // uniform: every tile is taken
   const uint32_t base = tile * uint32_t(kTile);
   const uint32_t shift = pass * 8;
 
@@ -427,6 +436,10 @@ k_onesweep(const uint32_t* __restrict__ kin,
       if (kPairs)
         vout[o] = s_vals[i];
     }
+  }
+  if (!looping)
+    break;
+  __syncthreads(); // the next tile reuses the shared arrays
   }
 }
 
@@ -1946,21 +1959,24 @@ launch_sort(uint32_t n, bool pairs, uint32_t epoch_base, const BuildBuffers& b, 
   uint32_t* vb = b.vals_b;
   const uint32_t spin = b.spin_limit ? b.spin_limit : kSpinLimit;
   const uint32_t wx = b.wait_xor;
+  // after a bucket sort the passes only run when it gave up: one wave of CTAs
+  // looping over the tiles instead of one CTA per tile
+  const uint32_t grid = (msd && b.sort_ctas && tiles > 4 * b.sort_ctas) ? 4 * b.sort_ctas : tiles;
   for (uint32_t pass = 0; pass < passes; pass++) {
     const uint32_t epoch = epoch_base + pass;
     if (pairs) {
       if (pass == 0)
         CUDA_TRY(launch_pdl(k_onesweep<true, true>, tiles, kSortThreads, 0, s, ka, kb, nullptr, vb, n, pass, epoch,
-                            b.lookback, b.state, false, spin, wx));
+                            b.lookback, b.state, false, spin, wx, tiles));
       else
         CUDA_TRY(launch_pdl(k_onesweep<true, false>, tiles, kSortThreads, 0, s, ka, kb, va, vb, n, pass, epoch,
-                            b.lookback, b.state, false, spin, wx));
+                            b.lookback, b.state, false, spin, wx, tiles));
     } else if (small) {
-      CUDA_TRY(launch_pdl(k_onesweep<false, false, kSmallTileItems>, tiles, kSortThreads, 0, s, ka, kb, nullptr,
-                          nullptr, n, pass, epoch, b.lookback, b.state, msd, spin, wx));
+      CUDA_TRY(launch_pdl(k_onesweep<false, false, kSmallTileItems>, grid, kSortThreads, 0, s, ka, kb, nullptr,
+                          nullptr, n, pass, epoch, b.lookback, b.state, msd, spin, wx, tiles));
     } else {
-      CUDA_TRY(launch_pdl(k_onesweep<false, false>, tiles, kSortThreads, 0, s, ka, kb, nullptr, nullptr, n, pass, epoch,
-                          b.lookback, b.state, msd, spin, wx));
+      CUDA_TRY(launch_pdl(k_onesweep<false, false>, grid, kSortThreads, 0, s, ka, kb, nullptr, nullptr, n, pass, epoch,
+                          b.lookback, b.state, msd, spin, wx, tiles));
     }
     std::swap(ka, kb);
     std::swap(va, vb);

@@ -300,16 +300,17 @@ def test_dump_and_reload_round_trip(lib_built, tmp_path):
         lb.BVH.load(tmp_path / "bad.npz")
 
 
-@pytest.mark.parametrize("kind", ["uniform", "dense_bucket", "over_bucket", "crowded", "all_equal"])
-def test_large_builds_with_crowded_buckets_match_oracle(ctx, port, kind):
+@pytest.mark.parametrize("kind,n", [("uniform", 1_600_000), ("dense_bucket", 1_600_000), ("over_bucket", 1_600_000),
+                                    ("crowded", 1_600_000), ("all_equal", 1_600_000), ("over_bucket", 3_000_000)])
+def test_large_builds_with_crowded_buckets_match_oracle(ctx, port, kind, n):
     """Keys-only builds of at least 1.5M primitives sort by buckets of the
     top 12 code bits when every bucket holds at most 20,480 codes and by the
     radix passes otherwise. A uniform soup and one with a bucket filled to
     19,543 codes (18,000 of them equal) take the first path; 1,000 more
     equal codes (20,542 in the bucket), a scene whose codes crowd one bucket,
-    and one whose codes are all equal take the second. All match the
-    oracle."""
-    n = 1_600_000
+    and one whose codes are all equal take the second. At 3M primitives the
+    radix passes run on one wave of CTAs that loop over the tiles. All match
+    the oracle."""
     if kind in ("uniform", "dense_bucket", "over_bucket"):
         t = scenes.soup_large(n, seed=90)
         if kind != "uniform":
