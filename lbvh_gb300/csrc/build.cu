@@ -1455,10 +1455,11 @@ k_tree_merge(Leaf leaf,
 //      (k_bounds); the CTAs' partial bounds are combined through distributed
 //      shared memory;
 //   2. the Morton codes (k_morton);
-//   3. four stable 8-bit LSD passes over the cluster: each CTA ranks its keys
-//      per warp (__match_any_sync), publishes its digit counts, reads every
-//      CTA's counts to find its keys' global positions, and stores each key
-//      into the shared memory of the CTA that owns that position;
+//   3. three stable 10-bit LSD passes over the cluster (the codes are 30
+//      bits): each CTA ranks its keys per warp (__match_any_sync), publishes
+//      its digit counts, reads every CTA's counts to find its keys' global
+//      positions, and stores each key into the shared memory of the CTA that
+//      owns that position;
 //   4. the local tree phase over the CTA's 1,024 slots (local_walks), with the
 //      neighbours' edge codes read remotely, its pieces kept in shared memory;
 //   5. CTA 0 gathers every CTA's pieces and merges them to the root
