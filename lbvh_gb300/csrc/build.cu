@@ -1455,11 +1455,13 @@ k_tree_merge(Leaf leaf,
 //      (k_bounds); the CTAs' partial bounds are combined through distributed
 //      shared memory;
 //   2. the Morton codes (k_morton);
-//   3. three stable 10-bit LSD passes over the cluster (the codes are 30
-//      bits): each CTA ranks its keys per warp (__match_any_sync), publishes
-//      its digit counts, reads every CTA's counts to find its keys' global
-//      positions, and stores each key into the shared memory of the CTA that
-//      owns that position;
+//   3. a stable sort over the cluster: each CTA sorts its (code, index) pairs
+//      with a bitonic network and tabulates where each value of the codes'
+//      top 10 bits starts in its sorted run; a code's global position is its
+//      rank in its own run plus, for every other CTA, the start of its bucket
+//      there and a binary search inside that bucket (ties go to the lower
+//      CTA, which keeps equal codes in index order); each code is stored into
+//      the shared memory of the CTA that owns its position;
 //   4. the local tree phase over the CTA's 1,024 slots (local_walks), with the
 //      neighbours' edge codes read remotely, its pieces kept in shared memory;
 //   5. CTA 0 gathers every CTA's pieces and merges them to the root
@@ -1484,7 +1486,7 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   extern __shared__ __align__(32) unsigned char smem[];
   Box* s_box = reinterpret_cast<Box*>(smem + kSmBox);
   uint32_t* s_key = reinterpret_cast<uint32_t*>(smem + kSmKey);
-  __shared__ uint32_t s_hist[1024], s_base[1024], s_wsum[32];
+  __shared__ uint16_t s_tab[1025]; // the CTA's sorted run by bucket (step 3)
   PieceRec* s_piece = reinterpret_cast<PieceRec*>(smem + kSmPiece);
   unsigned char* u = smem + kSmUnion;
   __shared__ ArgBox s_part[kSmallThreads / 32];
@@ -1550,85 +1552,78 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   if (valid)
     key_cur[tid] = morton_of(bx, s_lo[0], s_lo[1], s_lo[2], s_scale[0], s_scale[1], s_scale[2]);
 
-  // ---- 3. three stable 10-bit LSD passes over the cluster (codes are 30 bits) ----
-  uint16_t* s_wcnt = reinterpret_cast<uint16_t*>(u); // [32 warps][1024 digits]
-  for (uint32_t k = tid; k < 32 * 1024 / 2; k += kSmallThreads)
-    reinterpret_cast<uint32_t*>(s_wcnt)[k] = 0;
-  for (int pass = 0; pass < 3; pass++) {
-    __syncthreads();
-    const uint32_t key = valid ? key_cur[tid] : 0u;
-    const uint32_t d = (key >> (10 * pass)) & 1023u;
-    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 1024u + lane);
-    const uint32_t rank_w = __popc(peers & ((1u << lane) - 1u));
-    if (valid && rank_w == 0)
-      s_wcnt[warp * 1024 + d] = uint16_t(__popc(peers));
-    __syncthreads();
-    { // digit tid: the warps' exclusive prefix, and the CTA's count
-      uint32_t run = 0;
-#pragma unroll 8
-      for (int w = 0; w < 32; w++) {
-        const uint32_t c = s_wcnt[w * 1024 + tid];
-        s_wcnt[w * 1024 + tid] = uint16_t(run);
-        run += c;
-      }
-      s_hist[tid] = run;
-    }
-    cluster.sync(); // every CTA's digit counts are complete
-    uint32_t tot = 0, before = 0;
-    { // every CTA's count of this digit, read in parallel
-      uint32_t h[kSmallMaxCtas];
-#pragma unroll
-      for (uint32_t q = 0; q < kSmallMaxCtas; q++)
-        h[q] = q < C ? cluster.map_shared_rank(s_hist, q)[tid] : 0u;
-#pragma unroll
-      for (uint32_t q = 0; q < kSmallMaxCtas; q++) {
-        tot += h[q];
-        before += q < r ? h[q] : 0u;
-      }
-    }
-    { // exclusive scan of the 1,024 digit totals
-      uint32_t x = tot;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= uint32_t(o))
-          x += y;
-      }
-      if (lane == 31)
-        s_wsum[warp] = x;
-      __syncthreads();
-      if (warp == 0) {
-        const uint32_t w = s_wsum[lane];
-        uint32_t t = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-          if (lane >= uint32_t(o))
-            t += y;
+  // ---- 3. the stable sort: each CTA sorts its (code, index) pairs, then
+  //      every code finds its position among all CTAs' sorted runs ----
+  // 3a. bitonic sort of the CTA's pairs, distinct since the indices are
+  //     (exchanges of distance >= 32 through shared memory, two buffers;
+  //     the rest by shuffles); past-the-end lanes sort last
+  unsigned long long* s_bit = reinterpret_cast<unsigned long long*>(u); // [2][kSmallSlots]
+  {
+    unsigned long long v = valid ? (static_cast<unsigned long long>(key_cur[tid]) << 32) | (b0 + tid) : ~0ull;
+    int buf = 0;
+    for (uint32_t k = 2; k <= kSmallSlots; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        unsigned long long o;
+        if (j >= 32) {
+          s_bit[buf * kSmallSlots + tid] = v;
+          __syncthreads();
+          o = s_bit[buf * kSmallSlots + (tid ^ j)];
+          buf ^= 1;
+        } else {
+          o = __shfl_xor_sync(0xffffffffu, v, j);
         }
-        s_wsum[lane] = t - w;
+        const bool keep_min = ((tid & j) == 0) == ((tid & k) == 0);
+        v = keep_min ? (o < v ? o : v) : (o < v ? v : o);
       }
-      __syncthreads();
-      s_base[tid] = x - tot + s_wsum[warp] + before;
-    }
-    __syncthreads();
-    if (valid) {
-      const uint32_t pos = s_base[d] + s_wcnt[warp * 1024 + d] + rank_w; // < n by construction
-      if (pos < n)
-        cluster.map_shared_rank(key_nxt, pos / kSmallSlots)[pos % kSmallSlots] = key;
-      else
-        atomicOr(&st->error, kErrBadTopology);
-    }
-    // every key has landed and every count has been read once all CTAs
-    // arrive; the next pass's warp counts are cleared meanwhile
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    for (uint32_t k = tid; k < 32 * 1024 / 2; k += kSmallThreads)
-      reinterpret_cast<uint32_t*>(s_wcnt)[k] = 0;
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-    uint32_t* t = key_cur;
-    key_cur = key_nxt;
-    key_nxt = t;
+    if (valid)
+      key_nxt[tid] = uint32_t(v >> 32); // the CTA's run, in order
   }
+  __syncthreads();
+  // 3b. the run's bucket table: s_tab[t] = the run's codes below bucket t
+  //     (t = the top 10 code bits), for t = 0..1024
+  for (uint32_t t = tid; t <= 1024; t += kSmallThreads) {
+    uint32_t lo = 0, hi = cnt; // first run index whose bucket is >= t
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if ((key_nxt[mid] >> 20) < t)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    s_tab[t] = uint16_t(lo);
+  }
+  cluster.sync(); // every CTA's run and table are complete
+  // 3c. a code's position: its rank in its own run plus, in each other run,
+  //     the codes before it -- below its bucket from the table, then inside
+  //     the bucket by binary search: codes <= its own in runs of lower index
+  //     (their primitives come first), codes < its own in later runs
+  if (valid) {
+    const uint32_t code = key_nxt[tid];
+    const uint32_t t = code >> 20;
+    uint32_t pos = tid;
+#pragma unroll
+    for (uint32_t q = 0; q < kSmallMaxCtas; q++) {
+      if (q >= C || q == r)
+        continue;
+      const uint16_t* tab = cluster.map_shared_rank(s_tab, q);
+      const uint32_t* run = cluster.map_shared_rank(key_nxt, q);
+      uint32_t lo = tab[t], hi = tab[t + 1];
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t c = run[mid];
+        if (q < r ? c <= code : c < code)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      pos += lo;
+    }
+    if (pos < n)
+      cluster.map_shared_rank(key_cur, pos / kSmallSlots)[pos % kSmallSlots] = code;
+    else
+      atomicOr(&st->error, kErrBadTopology); // < n by construction
+  }
+  cluster.sync(); // every code has landed; every run and table has been read
 
   // ---- 4. local tree phase over the CTA's slots ----
   int* s_delta = reinterpret_cast<int*>(u);
