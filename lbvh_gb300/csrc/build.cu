@@ -1455,13 +1455,13 @@ k_tree_merge(Leaf leaf,
 //      (k_bounds); the CTAs' partial bounds are combined through distributed
 //      shared memory;
 //   2. the Morton codes (k_morton);
-//   3. a stable sort over the cluster: each CTA sorts its (code, index) pairs
-//      with a bitonic network and tabulates where each value of the codes'
-//      top 10 bits starts in its sorted run; a code's global position is its
-//      rank in its own run plus, for every other CTA, the start of its bucket
-//      there and a binary search inside that bucket (ties go to the lower
-//      CTA, which keeps equal codes in index order); each code is stored into
-//      the shared memory of the CTA that owns its position;
+//   3. a sort over the cluster: each CTA sorts its codes with a bitonic
+//      network and tabulates where each value of the codes' top 10 bits
+//      starts in its sorted run; a code's global position is its rank in its
+//      own run plus, for every other CTA, the start of its bucket there and a
+//      binary search inside that bucket (ties go to the lower CTA, so every
+//      position is taken once); each code is stored into the shared memory
+//      of the CTA that owns its position;
 //   4. the local tree phase over the CTA's 1,024 slots (local_walks), with the
 //      neighbours' edge codes read remotely, its pieces kept in shared memory;
 //   5. CTA 0 gathers every CTA's pieces and merges them to the root
@@ -1552,18 +1552,19 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   if (valid)
     key_cur[tid] = morton_of(bx, s_lo[0], s_lo[1], s_lo[2], s_scale[0], s_scale[1], s_scale[2]);
 
-  // ---- 3. the stable sort: each CTA sorts its (code, index) pairs, then
-  //      every code finds its position among all CTAs' sorted runs ----
-  // 3a. bitonic sort of the CTA's pairs, distinct since the indices are
-  //     (exchanges of distance >= 32 through shared memory, two buffers;
-  //     the rest by shuffles); past-the-end lanes sort last
-  unsigned long long* s_bit = reinterpret_cast<unsigned long long*>(u); // [2][kSmallSlots]
+  // ---- 3. the sort: each CTA sorts its codes, then every code finds its
+  //      position among all CTAs' sorted runs ----
+  // 3a. bitonic sort of the CTA's codes (only the codes are kept, so equal
+  //     codes are interchangeable; exchanges of distance >= 32 through
+  //     shared memory, two buffers; the rest by shuffles); past-the-end
+  //     lanes carry ~0, above every 30-bit code, and sort last
+  uint32_t* s_bit = reinterpret_cast<uint32_t*>(u); // [2][kSmallSlots]
   {
-    unsigned long long v = valid ? (static_cast<unsigned long long>(key_cur[tid]) << 32) | (b0 + tid) : ~0ull;
+    uint32_t v = valid ? key_cur[tid] : ~0u;
     int buf = 0;
     for (uint32_t k = 2; k <= kSmallSlots; k <<= 1)
       for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-        unsigned long long o;
+        uint32_t o;
         if (j >= 32) {
           s_bit[buf * kSmallSlots + tid] = v;
           __syncthreads();
@@ -1573,10 +1574,10 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
           o = __shfl_xor_sync(0xffffffffu, v, j);
         }
         const bool keep_min = ((tid & j) == 0) == ((tid & k) == 0);
-        v = keep_min ? (o < v ? o : v) : (o < v ? v : o);
+        v = keep_min ? min(o, v) : max(o, v);
       }
     if (valid)
-      key_nxt[tid] = uint32_t(v >> 32); // the CTA's run, in order
+      key_nxt[tid] = v; // the CTA's run, in order
   }
   __syncthreads();
   // 3b. the run's bucket table: s_tab[t] = the run's codes below bucket t
@@ -1595,8 +1596,8 @@ k_small_build(Leaf leaf, uint32_t n, uint32_t* __restrict__ codes_out, Node* __r
   cluster.sync(); // every CTA's run and table are complete
   // 3c. a code's position: its rank in its own run plus, in each other run,
   //     the codes before it -- below its bucket from the table, then inside
-  //     the bucket by binary search: codes <= its own in runs of lower index
-  //     (their primitives come first), codes < its own in later runs
+  //     the bucket by binary search: codes <= its own in runs of lower index,
+  //     codes < its own in later runs (equal codes thus take distinct places)
   if (valid) {
     const uint32_t code = key_nxt[tid];
     const uint32_t t = code >> 20;

@@ -173,7 +173,7 @@ constexpr size_t kSmMergeSlot = kSmMergeR + kSmallMergeCap * 4;
 constexpr size_t kSmMergeD = kSmMergeSlot + kSmallMergeCap * 4;
 constexpr size_t kSmMergeOut = kSmMergeD + kSmallMergeCap;
 constexpr size_t kSmMerge = kSmMergeOut + kMergeOut * 48;
-constexpr size_t kSmSort = 2 * kSmallSlots * 8; // uint64[2][kSmallSlots]: bitonic exchange buffers
+constexpr size_t kSmSort = 2 * kSmallSlots * 4; // uint32[2][kSmallSlots]: bitonic exchange buffers
 constexpr size_t kSmallSmem =
   kSmUnion + (kSmMerge > kSmTree ? (kSmMerge > kSmSort ? kSmMerge : kSmSort) : (kSmTree > kSmSort ? kSmTree : kSmSort));
 static_assert(kSmUnion % 32 == 0 && kSmPiece % 32 == 0 && kSmTreeRec % 32 == 0, "small build smem alignment");
