@@ -183,6 +183,21 @@ tri_test(const RayCtx& r, const Tri* __restrict__ tris, uint32_t p, float& t, fl
   return false;
 }
 
+// One traversal node in two 256-bit loads (sm_100 and later; each half is
+// 32-byte aligned: the node arrays come from cudaMallocAsync and hold
+// 64-byte records). Read-only for the kernel's lifetime, hence .nc.
+__device__ __forceinline__ void
+load_wide(const WideNode* p, float4& A, float4& B, float4& C, float4& D)
+{
+  const float4* q = reinterpret_cast<const float4*>(p);
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(A.x), "=f"(A.y), "=f"(A.z), "=f"(A.w), "=f"(B.x), "=f"(B.y), "=f"(B.z), "=f"(B.w)
+      : "l"(q));
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(C.x), "=f"(C.y), "=f"(C.z), "=f"(C.w), "=f"(D.x), "=f"(D.y), "=f"(D.z), "=f"(D.w)
+      : "l"(q + 2));
+}
+
 // ---------------------------------------------------------------------------
 // Traversal layout: node i = {left box, right box, left, right} in 64 bytes.
 // A leaf child's box slot is unused (the reference tests leaf triangles
@@ -416,8 +431,8 @@ k_trace(const WideNode* __restrict__ wnodes,
     // ---- one node visit (lbvh.h:1902-1938) for the lanes whose previous
     // visit is complete; cur passed the cull test ----
     if (busy && !pend) {
-      const float4* w = reinterpret_cast<const float4*>(wnodes + nb + cur.x);
-      const float4 A = __ldg(w + 0), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+      float4 A, B, C, D;
+      load_wide(wnodes + nb + cur.x, A, B, C, D);
       const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
       bool lhit = false, rhit = false;
       float lt = inf, rt = inf;
