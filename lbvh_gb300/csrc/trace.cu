@@ -14,7 +14,7 @@
 //
 // GB300 mapping:
 //   * a traversal copy of the tree in which each internal node carries both
-//     children's boxes (64 bytes, four 16-byte loads from one line), built
+//     children's boxes (64 bytes, two 32-byte loads from one line), built
 //     once per build by k_repack;
 //   * persistent warps: a lane whose ray has finished takes the next ray of
 //     its warp's batch (ballot + shuffle), and a warp fetches a new batch of
@@ -759,8 +759,8 @@ k_trace_spheres(const WideNode* __restrict__ wnodes,
       const uint2 e = stack[--sp];
       if (best.t < __uint_as_float(e.y))
         continue;
-      const float4* w = reinterpret_cast<const float4*>(wnodes + e.x);
-      const float4 A = __ldg(w + 0), B = __ldg(w + 1), C = __ldg(w + 2), D = __ldg(w + 3);
+      float4 A, B, C, D;
+      load_wide(wnodes + e.x, A, B, C, D);
       const uint32_t left = __float_as_uint(D.x), right = __float_as_uint(D.y);
       bool lhit = false, rhit = false;
       float lt = inf, rt = inf;
