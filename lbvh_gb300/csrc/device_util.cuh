@@ -112,12 +112,18 @@ boundary_delta(const uint32_t* __restrict__ codes, uint32_t n, uint32_t k)
   return a == b ? int(__clz(k ^ (k + 1))) + 32 : int(__clz(a ^ b));
 }
 
+// One node record in one 256-bit store (sm_100 and later): every node array
+// the build kernels write is 32-byte aligned (cudaMallocAsync, or a caller's
+// array that the allocation-free entry point checks). The memory clobber
+// keeps the store ahead of the release that may follow it.
 __device__ __forceinline__ void
 store_node(Node* __restrict__ nodes, uint32_t idx, const Box& b, uint32_t l, uint32_t r)
 {
-  float4* dst = reinterpret_cast<float4*>(nodes + idx);
-  __stcg(dst + 0, make_float4(b.lo[0], b.lo[1], b.lo[2], b.hi[0]));
-  __stcg(dst + 1, make_float4(b.hi[1], b.hi[2], __uint_as_float(l), __uint_as_float(r)));
+  asm volatile("st.global.cg.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+               :
+               : "l"(nodes + idx), "f"(b.lo[0]), "f"(b.lo[1]), "f"(b.lo[2]), "f"(b.hi[0]), "f"(b.hi[1]), "f"(b.hi[2]),
+                 "f"(__uint_as_float(l)), "f"(__uint_as_float(r))
+               : "memory");
 }
 
 // Arrival at a device-scope slot: swaps in `v` and returns the previous word,
