@@ -1216,6 +1216,16 @@ lbvh_server_create(const lbvh_server_config* cfg, lbvh_server** out)
         destroy_all(s);
         return LBVH_ERR_DEVICE;
       }
+      // Workers build with the multi-kernel path only. The one-launch small
+      // build is a thread-block cluster that needs up to 16 SMs, each with
+      // about 162 KB of shared memory free, at the same moment; with the
+      // other workers' kernels running on every SM it can wait long enough
+      // to stall the whole request stream. The nodes are the same either way.
+      if (lbvh_ctx_set_param(w->ctx, LBVH_PARAM_SMALL_BUILD_MAX, 0) != LBVH_OK) {
+        s->workers.push_back(std::move(w));
+        destroy_all(s);
+        return LBVH_ERR_DEVICE;
+      }
       s->workers.push_back(std::move(w));
     }
     {
