@@ -309,8 +309,12 @@ k_onesweep(const uint32_t* __restrict__ kin,
 
   // digits are recomputed from the keys where needed (fewer live registers)
   const uint32_t first = base + uint32_t(warp) * (32 * kItems) + lane;
+  // the top pass of 30-bit codes has 6-bit digits; ranking, counters and
+  // positions all use the same masked digit, so the tile's positions stay
+  // inside the tile whatever words it is given
+  const uint32_t dmask = pass == 3 ? 63u : 255u;
   auto digit = [&](uint32_t kv, int k) -> uint32_t {
-    return first + uint32_t(k) * 32 < n ? (kv >> shift) & 255u : 256u; // 256: not a key, in no bucket
+    return first + uint32_t(k) * 32 < n ? (kv >> shift) & dmask : 256u; // 256: not a key, in no bucket
   };
   uint32_t key[kItems], val[kPairs ? kItems : 1], rank[kItems];
 #pragma unroll
@@ -327,7 +331,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
   // the top pass has 6-bit digits); a partial tile also masks out its
   // non-keys.
   const uint32_t lt_mask = (1u << lane) - 1u;
-  const uint32_t digit_bits = pass == 3 ? 6u : 8u; // codes are 30 bits
+  const uint32_t digit_bits = pass == 3 ? 6u : 8u; // the bits of dmask
   const bool full_tile = base + uint32_t(kTile) <= n;
 #pragma unroll
   for (int k = 0; k < kItems; k++) {
@@ -429,7 +433,7 @@ k_onesweep(const uint32_t* __restrict__ kin,
   const uint32_t tile_n = min(uint32_t(kTile), n - base);
   for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
     const uint32_t k = s_keys[i];
-    const uint32_t d = (k >> shift) & 255u;
+    const uint32_t d = (k >> shift) & dmask;
     const uint32_t o = s_gbase[d] + i - s_tile_start[d];
     if (o < n) { // always true unless a look-back wait gave up
       kout[o] = k;

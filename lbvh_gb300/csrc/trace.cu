@@ -397,7 +397,7 @@ k_trace(const WideNode* __restrict__ wnodes,
           }
           if (id < m) {
             if (order) // rays taken in a sorted order; each hit still goes to its ray's slot
-              id = __ldg(order + id);
+              id = min(__ldg(order + id), m - 1); // < m unless the ray sort gave up (error reported)
             ray = id;
             if (kHostHits)
               buf = id_buf;
