@@ -384,13 +384,14 @@ build_common(lbvh_ctx* c, const float* prims, size_t n, uint32_t flags, lbvh_bvh
   b.tile_keys = c->tile_keys;
   b.walk_fused = c->walk_fused;
   if (b.msd) {
-    // ranges of at least one partition tile, a few per SM; their count rows
+    // ranges of at least 8,192 codes, a few per SM; their count rows
     // (ranges x 16 KB <= 2n + 16 KB) live in vals_a, unused by keys-only sorts
-    const uint32_t want = std::min(uint32_t(c->num_sms) * 8, ceil_div_u32(nn, kPartTile));
+    const uint32_t want = std::min(uint32_t(c->num_sms) * 8, ceil_div_u32(nn, 8192u));
     b.msd_range = (ceil_div_u32(nn, want) + 255u) & ~255u;
     b.msd_ranges = ceil_div_u32(nn, b.msd_range);
-    // the partition: about two CTAs per SM, each over `group` whole ranges
-    b.msd_group = ceil_div_u32(b.msd_ranges, uint32_t(c->num_sms) * 2);
+    // the partition: about one CTA per SM (its 160 KB of shared memory allow
+    // no second), each over `group` whole ranges
+    b.msd_group = ceil_div_u32(b.msd_ranges, uint32_t(c->num_sms));
     b.sort_ctas = uint32_t(c->num_sms);
     b.top_rows = b.vals_a;
   }

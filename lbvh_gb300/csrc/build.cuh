@@ -37,8 +37,8 @@ constexpr int kTopBits = 12, kTopBuckets = 1 << kTopBits;
 // 0-12, a stable one by bits 13-17
 constexpr int kFirstBits = 13, kFirstDigits = 1 << kFirstBits;
 constexpr int kSecondBits = 5, kSecondDigits = 1 << kSecondBits;
-constexpr int kPartThreads = 512, kPartItems = 16;
-constexpr int kPartTile = kPartThreads * kPartItems; // 8192 keys per partition tile
+constexpr int kPartThreads = 1024, kPartItems = 16;
+constexpr int kPartTile = kPartThreads * kPartItems; // 16384 keys per partition tile (one CTA per SM)
 constexpr size_t kPartSmem = (size_t(2) * kTopBuckets + 2 * size_t(kPartTile)) * 4;
 constexpr int kBucketThreads = 1024, kBucketItems = 8;
 constexpr int kBucketChunk = kBucketThreads * kBucketItems; // 8192 keys ranked per step
